@@ -1,0 +1,212 @@
+/*
+ * pflbm.h - C ABI of the GB300-native phase-field lattice-Boltzmann hot path.
+ *
+ * The reference (phaseFieldLBM) has no plugin or FFI layer: its seam is the
+ * kernel set declared in src/LBMIncludes.cuh:121-136, driven by the time loop
+ * in src/main.cu:163-188 and specialised at compile time by -DVS_<set> and
+ * -D<CASE> (src/constants.cuh:39-49). This header replaces that seam with a
+ * runtime-configured C interface: every compile-time constant of
+ * src/constants.cuh:80-143 becomes a field of pflbm_config, and the kernels of
+ * src/phaseField.cuh, src/lbm.cu, src/BoundaryConditions.cuh,
+ * src/initialConditions.cu and src/derivedFields/ sit behind pflbm_init /
+ * pflbm_step / pflbm_get_field.
+ *
+ * Conventions
+ *   - Every function returns an int status (PFLBM_OK == 0). On failure a
+ *     thread-local message is available from pflbm_last_error(). Nothing
+ *     aborts or traps (the reference calls std::abort, src/cuda/errorCheck.cuh:36-42).
+ *   - The library owns all device memory; callers own host buffers.
+ *   - One simulation handle must not be used from two threads at once.
+ *   - Fields are SoA, x fastest: index = x + nx*(y + ny*z), as
+ *     src/functions/deviceFunctions.cuh:33-39. The outer one-node shell is a
+ *     ghost layer exactly as in the reference (guard, deviceFunctions.cuh:50-61).
+ */
+#ifndef PFLBM_H
+#define PFLBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFLBM_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+enum pflbm_status {
+    PFLBM_OK = 0,
+    PFLBM_ERR_INVALID_ARG = 1,   /* bad pointer, size or config value        */
+    PFLBM_ERR_CUDA = 2,          /* a CUDA runtime call failed               */
+    PFLBM_ERR_OUT_OF_MEMORY = 3, /* device allocation failed                 */
+    PFLBM_ERR_STATE = 4,         /* call out of order (e.g. step before init)*/
+    PFLBM_ERR_DIVERGED = 5,      /* NaN/Inf found by the diagnostics         */
+    PFLBM_ERR_UNSUPPORTED = 6,   /* feature not available in this build      */
+    PFLBM_ERR_IO = 7,            /* file output failed                       */
+    PFLBM_ERR_DEVICE = 8         /* a kernel reported an error flag          */
+};
+
+/* ---- selectors (src/constants.cuh:39-55, src/cuda/precision.cuh:26-56) - */
+enum pflbm_flow_case { PFLBM_CASE_DROPLET = 0, PFLBM_CASE_JET = 1 };
+enum pflbm_velocity_set { PFLBM_VS_D3Q19 = 19, PFLBM_VS_D3Q27 = 27 };
+enum pflbm_storage {
+    PFLBM_STORAGE_FP32 = 0, /* plain path: f, g stored FP32                       */
+    PFLBM_STORAGE_FP16 = 1, /* f as scaled (f_i - w_i)/w_i in FP16, phase flux FP16 */
+    PFLBM_STORAGE_BF16 = 2, /* same layout in BF16                                */
+    PFLBM_STORAGE_FP64 = 3  /* all arithmetic and storage FP64 (error oracle run) */
+};
+enum pflbm_inflow_noise {
+    PFLBM_NOISE_GAUSSIAN_UXY = 0, /* reference: Box-Muller on ux,uy, sd = amp*u_inf
+                                     (src/BoundaryConditions.cuh:58-69)          */
+    PFLBM_NOISE_UNIFORM_UZ = 1    /* uz = u_inf*(1 + amp*xi), xi ~ U[-1,1) from the
+                                     same counter hash, salted by seed           */
+};
+
+/* Optional per-step derived fields (src/derivedFields/DerivedFields.cuh:172-199). */
+enum pflbm_flags {
+    PFLBM_FLAG_TIME_AVERAGE = 1u << 0,    /* avg_phi, avg_ux, avg_uy, avg_uz        */
+    PFLBM_FLAG_REYNOLDS_MOMENTS = 1u << 1,/* avg_uxux ... avg_uyuz                  */
+    PFLBM_FLAG_VORTICITY = 1u << 2        /* vort_x/y/z/mag (computed on demand)    */
+};
+
+/* Field identifiers: same order as host::FieldID (src/fileIO/fields.cuh:33-68). */
+enum pflbm_field_id {
+    PFLBM_FIELD_RHO = 0, PFLBM_FIELD_UX, PFLBM_FIELD_UY, PFLBM_FIELD_UZ,
+    PFLBM_FIELD_PXX, PFLBM_FIELD_PYY, PFLBM_FIELD_PZZ,
+    PFLBM_FIELD_PXY, PFLBM_FIELD_PXZ, PFLBM_FIELD_PYZ,
+    PFLBM_FIELD_PHI = 10, PFLBM_FIELD_NORMX, PFLBM_FIELD_NORMY, PFLBM_FIELD_NORMZ,
+    PFLBM_FIELD_IND, PFLBM_FIELD_FFX = 15, PFLBM_FIELD_FFY, PFLBM_FIELD_FFZ,
+    PFLBM_FIELD_AVG_PHI = 18, PFLBM_FIELD_AVG_UX, PFLBM_FIELD_AVG_UY, PFLBM_FIELD_AVG_UZ,
+    PFLBM_FIELD_AVG_UXUX = 22, PFLBM_FIELD_AVG_UYUY, PFLBM_FIELD_AVG_UZUZ,
+    PFLBM_FIELD_AVG_UXUY, PFLBM_FIELD_AVG_UXUZ, PFLBM_FIELD_AVG_UYUZ,
+    PFLBM_FIELD_VORT_X = 28, PFLBM_FIELD_VORT_Y, PFLBM_FIELD_VORT_Z, PFLBM_FIELD_VORT_MAG,
+    PFLBM_FIELD_C = 32, /* passive scalar: not built (the reference's is a trap stub) */
+    PFLBM_FIELD_COUNT = 33
+};
+
+/*
+ * Run-time configuration. Replaces the compile-time namespaces mesh::,
+ * physics::, relaxation:: and sponge:: (src/constants.cuh:80-143,
+ * src/functions/globalFunctions.cuh:260-461). pflbm_config_reference() fills
+ * it with the reference's own compile-time values.
+ */
+typedef struct pflbm_config {
+    uint32_t struct_size;      /* = sizeof(pflbm_config); checked by pflbm_create  */
+    int32_t flow_case;         /* pflbm_flow_case                                  */
+    int32_t velocity_set;      /* pflbm_velocity_set (hydrodynamics; phase is D3Q7) */
+    int32_t storage;           /* pflbm_storage                                    */
+    uint32_t nx, ny, nz;       /* mesh::nx/ny/nz, ghost shell included             */
+    int32_t radius;            /* mesh::radius: droplet radius / jet inlet radius  */
+    int32_t diam;              /* mesh::diam: jet inlet diameter (viscosity scale) */
+    float droplet_x_stretch;   /* droplet IC divides (x - cx) by this; the reference
+                                  uses 2 (ellipsoid, src/initialConditions.cu:74)  */
+    float center_offset[3];    /* droplet centre offset from ((n-1)/2, ...)        */
+    float u_inf;               /* physics::u_inf                                   */
+    float reynolds_water;      /* physics::reynolds_water (jet)                    */
+    float reynolds_oil;        /* physics::reynolds_oil (jet)                      */
+    float sigma;               /* surface tension coefficient                      */
+    float interface_width;     /* physics::interface_width                         */
+    float gamma;               /* sharpening coefficient in gamma*phi*(1-phi)       */
+    float tau;                 /* droplet relaxation time (physics::tau)           */
+    float sponge_gain;         /* sponge::K_gain (jet outflow sponge)              */
+    int32_t sponge_cells;      /* sponge thickness; < 0 means nz/12                 */
+    int32_t inflow_noise;      /* pflbm_inflow_noise                               */
+    float noise_amp;           /* 0.08 for the reference's Gaussian mode           */
+    uint32_t seed;             /* salt of the uniform inflow / initial noise       */
+    float init_noise;          /* +-amplitude of seeded uniform initial velocity   */
+    uint32_t flags;            /* pflbm_flags                                      */
+    int32_t device;            /* CUDA device; < 0: $GPU_INDEX or 0 (hostFunctions.cuh:117-150) */
+} pflbm_config;
+
+/* FP64 diagnostics over the interior nodes (the ghost shell is excluded). */
+typedef struct pflbm_diag {
+    uint64_t step;             /* number of completed steps                        */
+    double phi_mass;           /* sum phi                                          */
+    double rho_mass;           /* sum rho                                          */
+    double momentum[3];        /* sum rho*u                                        */
+    double max_speed;          /* max |u|                                          */
+    double rho_in, rho_out;    /* mean rho where phi > 0.9 / phi < 0.1             */
+    double laplace_dp;         /* cs2 * (rho_in - rho_out)                         */
+    uint64_t n_in, n_out;      /* node counts of the two classes                   */
+    uint64_t nonfinite;        /* count of NaN/Inf among rho, u, phi               */
+} pflbm_diag;
+
+typedef struct pflbm_sim pflbm_sim;
+
+/* Library identity. */
+int pflbm_abi_version(void);
+const char *pflbm_last_error(void);
+
+/* Fills cfg with the reference's compile-time defaults for (flow_case,
+ * velocity_set): src/constants.cuh:80-141 (JET 64x64x128, D=10, Re=We-scaled
+ * sigma; DROPLET 128^3, R=35, tau=0.55, sigma=0.03), gamma from
+ * src/constants.cuh:104-108, sponge from globalFunctions.cuh:260-292. */
+int pflbm_config_reference(pflbm_config *cfg, int32_t flow_case, int32_t velocity_set);
+
+/* Allocates every device field (src/fieldAllocate/FieldAllocate.cuh:47-66
+ * plus src/main.cu:56-79) and captures the per-step CUDA graph
+ * (src/cuda/CUDAGraph.cuh:35-58). */
+int pflbm_create(const pflbm_config *cfg, pflbm_sim **out);
+
+/* Initial conditions: setInitialDensity, setJet|setDroplet, setDistros
+ * (src/initialConditions.cu:33-138, src/main.cu:114-116). Resets the step
+ * counter and the derived-field averages. */
+int pflbm_init(pflbm_sim *sim);
+
+/* Overrides the initial rho, phi or velocity (field id RHO, PHI, UX, UY or
+ * UZ) with a host array of nx*ny*nz floats. f and the phase field are
+ * rebuilt from the equilibria (as setDistros does) before the next step.
+ * Valid only at step 0. */
+int pflbm_set_initial_field(pflbm_sim *sim, int32_t field_id, const float *host_src, size_t bytes);
+
+/* Advances nsteps time steps: one body of src/main.cu:163-176 each
+ * (graph, boundary conditions, derived fields), without a host sync per step.
+ * Returns after the device has finished. */
+int pflbm_step(pflbm_sim *sim, uint64_t nsteps);
+
+/* Same as pflbm_step but only enqueues the work on the simulation's stream. */
+int pflbm_step_async(pflbm_sim *sim, uint64_t nsteps);
+int pflbm_synchronize(pflbm_sim *sim);
+
+/* Runs nsteps time steps with every kernel launched on its own (no graph)
+ * between a pair of CUDA events on the simulation's stream. total_ms gets
+ * the elapsed time from the first to the last event; kernel_ms[k] gets the
+ * summed duration of kernel k of the step (0 = collide, 1 = phase) for
+ * k < n_kernels. Used for the roofline measurement; results are identical
+ * to pflbm_step. */
+int pflbm_step_profiled(pflbm_sim *sim, uint64_t nsteps, double *total_ms, double *kernel_ms, int32_t n_kernels);
+
+/* Number of completed steps. */
+int pflbm_current_step(const pflbm_sim *sim, uint64_t *step);
+
+/* Copies one nx*ny*nz float32 field, as the reference's arrays hold it after
+ * the last completed step (src/fileIO/fields.cuh:84-180), to host memory.
+ * bytes must be >= nx*ny*nz*4. */
+int pflbm_get_field(pflbm_sim *sim, int32_t field_id, void *host_dst, size_t bytes);
+
+/* Same field as FP64 (exact for FP64 storage runs, widened otherwise).
+ * bytes must be >= nx*ny*nz*8. No counterpart in the reference, whose
+ * scalar_t is float (src/cuda/precision.cuh:27). */
+int pflbm_get_field_f64(pflbm_sim *sim, int32_t field_id, double *host_dst, size_t bytes);
+
+/* FP64 reductions (mass, momentum, Laplace jump, NaN count). Returns
+ * PFLBM_ERR_DIVERGED when nonfinite > 0 (the diag is still filled). */
+int pflbm_reduce(pflbm_sim *sim, pflbm_diag *out);
+
+/* Writes <dir>/<name><step:06>.bin for each field and <dir>/step_<step:06>.vti
+ * that appends them (src/postProcess/PostProcess.cuh:43-261). */
+int pflbm_write_output(pflbm_sim *sim, const char *dir, const int32_t *field_ids, int32_t n_fields);
+
+/* Device bytes held by the simulation. */
+int pflbm_device_bytes(const pflbm_sim *sim, uint64_t *bytes);
+
+/* Number of CUDA kernels one time step launches (launch accounting). */
+int pflbm_kernels_per_step(const pflbm_sim *sim, int32_t *count);
+
+int pflbm_destroy(pflbm_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFLBM_H */

@@ -1,0 +1,336 @@
+"""GB300-native phase-field lattice-Boltzmann hot path (Python host mirror).
+
+The compute path is the CUDA library ``libpflbm.so`` behind the C ABI of
+``include/pflbm.h``; this module binds it with ctypes and mirrors the
+reference's driver vocabulary (flow case, velocity set, field names of
+src/fileIO/fields.cuh:33-68). There is no CPU fallback: if the library is
+missing or no CUDA device is present, creating a Simulation raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "CASE_DROPLET", "CASE_JET", "VS_D3Q19", "VS_D3Q27",
+    "STORAGE_FP32", "STORAGE_FP16", "STORAGE_BF16", "STORAGE_FP64",
+    "NOISE_GAUSSIAN_UXY", "NOISE_UNIFORM_UZ",
+    "FLAG_TIME_AVERAGE", "FLAG_REYNOLDS_MOMENTS", "FLAG_VORTICITY",
+    "FIELDS", "Config", "Diag", "PflbmError", "Simulation",
+    "load_library", "config_reference", "preset", "EXPORTED_SYMBOLS",
+]
+
+CASE_DROPLET, CASE_JET = 0, 1
+VS_D3Q19, VS_D3Q27 = 19, 27
+STORAGE_FP32, STORAGE_FP16, STORAGE_BF16, STORAGE_FP64 = 0, 1, 2, 3
+NOISE_GAUSSIAN_UXY, NOISE_UNIFORM_UZ = 0, 1
+FLAG_TIME_AVERAGE, FLAG_REYNOLDS_MOMENTS, FLAG_VORTICITY = 1, 2, 4
+
+# pflbm_field_id, in the order of host::FieldID (src/fileIO/fields.cuh:33-68)
+FIELDS = [
+    "rho", "ux", "uy", "uz", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz",
+    "phi", "normx", "normy", "normz", "ind", "fsx", "fsy", "fsz",
+    "avg_phi", "avg_ux", "avg_uy", "avg_uz",
+    "avg_uxux", "avg_uyuy", "avg_uzuz", "avg_uxuy", "avg_uxuz", "avg_uyuz",
+    "vort_x", "vort_y", "vort_z", "vort_mag", "c",
+]
+FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+
+EXPORTED_SYMBOLS = [
+    "pflbm_abi_version", "pflbm_last_error", "pflbm_config_reference", "pflbm_create",
+    "pflbm_init", "pflbm_set_initial_field", "pflbm_step", "pflbm_step_async",
+    "pflbm_synchronize", "pflbm_step_profiled", "pflbm_current_step", "pflbm_get_field", "pflbm_get_field_f64",
+    "pflbm_reduce", "pflbm_write_output", "pflbm_device_bytes", "pflbm_kernels_per_step",
+    "pflbm_destroy",
+]
+
+
+class Config(ctypes.Structure):
+    """pflbm_config (include/pflbm.h)."""
+
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("flow_case", ctypes.c_int32),
+        ("velocity_set", ctypes.c_int32),
+        ("storage", ctypes.c_int32),
+        ("nx", ctypes.c_uint32),
+        ("ny", ctypes.c_uint32),
+        ("nz", ctypes.c_uint32),
+        ("radius", ctypes.c_int32),
+        ("diam", ctypes.c_int32),
+        ("droplet_x_stretch", ctypes.c_float),
+        ("center_offset", ctypes.c_float * 3),
+        ("u_inf", ctypes.c_float),
+        ("reynolds_water", ctypes.c_float),
+        ("reynolds_oil", ctypes.c_float),
+        ("sigma", ctypes.c_float),
+        ("interface_width", ctypes.c_float),
+        ("gamma", ctypes.c_float),
+        ("tau", ctypes.c_float),
+        ("sponge_gain", ctypes.c_float),
+        ("sponge_cells", ctypes.c_int32),
+        ("inflow_noise", ctypes.c_int32),
+        ("noise_amp", ctypes.c_float),
+        ("seed", ctypes.c_uint32),
+        ("init_noise", ctypes.c_float),
+        ("flags", ctypes.c_uint32),
+        ("device", ctypes.c_int32),
+    ]
+
+    def copy(self) -> "Config":
+        c = Config()
+        ctypes.memmove(ctypes.byref(c), ctypes.byref(self), ctypes.sizeof(Config))
+        return c
+
+    def as_dict(self) -> dict:
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if name == "center_offset" else v
+        return d
+
+    @property
+    def nodes(self) -> int:
+        return int(self.nx) * int(self.ny) * int(self.nz)
+
+
+class Diag(ctypes.Structure):
+    """pflbm_diag (include/pflbm.h)."""
+
+    _fields_ = [
+        ("step", ctypes.c_uint64),
+        ("phi_mass", ctypes.c_double),
+        ("rho_mass", ctypes.c_double),
+        ("momentum", ctypes.c_double * 3),
+        ("max_speed", ctypes.c_double),
+        ("rho_in", ctypes.c_double),
+        ("rho_out", ctypes.c_double),
+        ("laplace_dp", ctypes.c_double),
+        ("n_in", ctypes.c_uint64),
+        ("n_out", ctypes.c_uint64),
+        ("nonfinite", ctypes.c_uint64),
+    ]
+
+
+class PflbmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pflbm error {code}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def load_library(path: str | os.PathLike | None = None, build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads libpflbm.so (building it with nvcc first if it is absent)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else _build.LIB
+    if not p.exists():
+        if not build_if_missing:
+            raise RuntimeError(f"{p} is missing; run phasefieldlbm_gb300.build.build()")
+        _build.build()
+    lib = ctypes.CDLL(str(p))
+    vp, i32, u32, u64, sz = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t
+    sig = {
+        "pflbm_abi_version": ([], ctypes.c_int),
+        "pflbm_last_error": ([], ctypes.c_char_p),
+        "pflbm_config_reference": ([ctypes.POINTER(Config), i32, i32], ctypes.c_int),
+        "pflbm_create": ([ctypes.POINTER(Config), ctypes.POINTER(vp)], ctypes.c_int),
+        "pflbm_init": ([vp], ctypes.c_int),
+        "pflbm_set_initial_field": ([vp, i32, vp, sz], ctypes.c_int),
+        "pflbm_step": ([vp, u64], ctypes.c_int),
+        "pflbm_step_async": ([vp, u64], ctypes.c_int),
+        "pflbm_synchronize": ([vp], ctypes.c_int),
+        "pflbm_current_step": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
+        "pflbm_step_profiled": ([vp, u64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), i32],
+                                ctypes.c_int),
+        "pflbm_get_field": ([vp, i32, vp, sz], ctypes.c_int),
+        "pflbm_get_field_f64": ([vp, i32, vp, sz], ctypes.c_int),
+        "pflbm_reduce": ([vp, ctypes.POINTER(Diag)], ctypes.c_int),
+        "pflbm_write_output": ([vp, ctypes.c_char_p, ctypes.POINTER(i32), i32], ctypes.c_int),
+        "pflbm_device_bytes": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
+        "pflbm_kernels_per_step": ([vp, ctypes.POINTER(i32)], ctypes.c_int),
+        "pflbm_destroy": ([vp], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if lib.pflbm_abi_version() != 1:
+        raise RuntimeError("libpflbm ABI version mismatch")
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _check(lib, rc: int):
+    if rc != 0:
+        raise PflbmError(rc, lib.pflbm_last_error().decode(errors="replace"))
+
+
+def config_reference(flow_case: int, velocity_set: int) -> Config:
+    """The reference's compile-time configuration (src/constants.cuh:80-141)."""
+    lib = load_library()
+    c = Config()
+    _check(lib, lib.pflbm_config_reference(ctypes.byref(c), flow_case, velocity_set))
+    return c
+
+
+@dataclass(frozen=True)
+class Preset:
+    name: str
+    description: str
+
+
+def preset(name: str, **overrides) -> Config:
+    """Configurations of the benchmark workloads (seeded synthetic cases).
+
+    droplet64        static droplet, D3Q19, 64^3 periodic, R=16, tau=0.6,
+                     sigma=0.01, gamma=0.05, spherical
+    jet_d3q27        turbulent jet, D3Q27, 128x128x512, D=16, u=0.05,
+                     Re=5000, We=500, gamma=0.05, uniform +-5% uz noise
+    jet_d3q19        the same jet in D3Q19
+    jet_precision    D3Q19 256x256x1024, D=32
+    jet_closure      D3Q19 128x128x512, D=16, Re=10000
+    """
+    lib = load_library()
+    c = Config()
+    if name == "droplet64":
+        _check(lib, lib.pflbm_config_reference(ctypes.byref(c), CASE_DROPLET, VS_D3Q19))
+        c.nx = c.ny = c.nz = 64
+        c.radius, c.diam = 16, 32
+        c.tau, c.sigma, c.gamma = 0.6, 0.01, 0.05
+        c.droplet_x_stretch = 1.0
+    elif name in ("jet_d3q27", "jet_d3q19", "jet_precision", "jet_closure"):
+        vs = VS_D3Q27 if name == "jet_d3q27" else VS_D3Q19
+        _check(lib, lib.pflbm_config_reference(ctypes.byref(c), CASE_JET, vs))
+        if name == "jet_precision":
+            c.nx, c.ny, c.nz, c.diam = 256, 256, 1024, 32
+        else:
+            c.nx, c.ny, c.nz, c.diam = 128, 128, 512, 16
+        c.radius = c.diam // 2
+        re = 10000.0 if name == "jet_closure" else 5000.0
+        c.reynolds_water = c.reynolds_oil = re
+        c.u_inf = 0.05
+        # sigma = u^2 D / We with We = 500, computed in float as constants.cuh:98
+        c.sigma = float(np.float32(np.float32(np.float32(c.u_inf) * np.float32(c.u_inf)) * np.float32(c.diam)) / np.float32(500.0))
+        c.gamma = 0.05
+        c.inflow_noise = NOISE_UNIFORM_UZ
+        c.noise_amp = 0.05
+        c.seed = 12345
+    else:
+        raise ValueError(f"unknown preset {name!r}")
+    for k, v in overrides.items():
+        if k == "center_offset":
+            for i in range(3):
+                c.center_offset[i] = v[i]
+        else:
+            setattr(c, k, v)
+    return c
+
+
+class Simulation:
+    """One simulation on one GPU (pflbm_create ... pflbm_destroy)."""
+
+    def __init__(self, config: Config, init: bool = True):
+        self.lib = load_library()
+        self.config = config.copy()
+        self.config.struct_size = ctypes.sizeof(Config)
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.pflbm_create(ctypes.byref(self.config), ctypes.byref(h)))
+        self._h = h
+        self.shape = (int(config.nz), int(config.ny), int(config.nx))
+        if init:
+            self.init()
+
+    # -- lifecycle -------------------------------------------------------
+    def init(self):
+        _check(self.lib, self.lib.pflbm_init(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.pflbm_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stepping --------------------------------------------------------
+    def step(self, n: int = 1):
+        _check(self.lib, self.lib.pflbm_step(self._h, int(n)))
+
+    def step_async(self, n: int = 1):
+        _check(self.lib, self.lib.pflbm_step_async(self._h, int(n)))
+
+    def step_profiled(self, n: int) -> tuple[float, list[float]]:
+        """Runs n steps with CUDA events around every kernel on the library's
+        stream; returns (total ms, [collide ms, phase ms])."""
+        tot = ctypes.c_double()
+        ks = (ctypes.c_double * 2)()
+        _check(self.lib, self.lib.pflbm_step_profiled(self._h, int(n), ctypes.byref(tot), ks, 2))
+        return float(tot.value), [float(ks[0]), float(ks[1])]
+
+    def synchronize(self):
+        _check(self.lib, self.lib.pflbm_synchronize(self._h))
+
+    @property
+    def current_step(self) -> int:
+        v = ctypes.c_uint64()
+        _check(self.lib, self.lib.pflbm_current_step(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    # -- fields ----------------------------------------------------------
+    def set_initial_field(self, name: str, values: np.ndarray):
+        a = np.ascontiguousarray(values, dtype=np.float32).reshape(-1)
+        _check(self.lib, self.lib.pflbm_set_initial_field(self._h, FIELD_ID[name], a.ctypes.data, a.nbytes))
+
+    def get_field(self, name: str, out: np.ndarray | None = None, dtype=np.float32) -> np.ndarray:
+        """Field as the reference's array holds it after the last step, shape (nz, ny, nx)."""
+        fid = FIELD_ID[name] if isinstance(name, str) else int(name)
+        if dtype == np.float64:
+            a = out if out is not None else np.empty(self.shape, np.float64)
+            _check(self.lib, self.lib.pflbm_get_field_f64(self._h, fid, a.ctypes.data, a.nbytes))
+        else:
+            a = out if out is not None else np.empty(self.shape, np.float32)
+            _check(self.lib, self.lib.pflbm_get_field(self._h, fid, a.ctypes.data, a.nbytes))
+        return a
+
+    def reduce(self) -> Diag:
+        d = Diag()
+        rc = self.lib.pflbm_reduce(self._h, ctypes.byref(d))
+        if rc not in (0, 5):
+            _check(self.lib, rc)
+        return d
+
+    def write_output(self, directory: str, fields=("rho", "uz")):
+        ids = (ctypes.c_int32 * len(fields))(*[FIELD_ID[f] for f in fields])
+        _check(self.lib, self.lib.pflbm_write_output(self._h, str(directory).encode(), ids, len(fields)))
+
+    @property
+    def device_bytes(self) -> int:
+        v = ctypes.c_uint64()
+        _check(self.lib, self.lib.pflbm_device_bytes(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    @property
+    def kernels_per_step(self) -> int:
+        v = ctypes.c_int32()
+        _check(self.lib, self.lib.pflbm_kernels_per_step(self._h, ctypes.byref(v)))
+        return int(v.value)

@@ -1,0 +1,167 @@
+"""Parity of the CUDA library (through the C ABI) with the CPU oracle.
+
+The oracle restates the reference's passes (src/phaseField.cuh, src/lbm.cu,
+src/BoundaryConditions.cuh) with its single-buffer push; the library runs the
+fused two-kernel pull step. Tolerances:
+  * FP64 storage vs FP64 oracle: rel. L2 <= 1e-10 on every field. Only
+    summation order differs, so this pins the semantics (ghost shell, BCs,
+    step order, noise) exactly.
+  * FP32 vs FP32 oracle: rel. L2 <= 1e-5 on rho, u and phi (the tolerance of
+    the FP32 plain path), 1e-3 on the small derived quantities Pi and F.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+BASIC = ("rho", "ux", "uy", "uz", "phi")
+ALL18 = ("rho", "ux", "uy", "uz", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz",
+         "phi", "normx", "normy", "normz", "ind", "fsx", "fsy", "fsz")
+
+
+def droplet_cfg(pf, vs, n=32, radius=8, stretch=2.0, **kw):
+    c = pf.config_reference(pf.CASE_DROPLET, vs)
+    c.nx = c.ny = c.nz = n
+    c.radius, c.diam = radius, 2 * radius
+    c.droplet_x_stretch = stretch
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def jet_cfg(pf, vs, nx=32, ny=32, nz=64, diam=10, noise=0, **kw):
+    c = pf.config_reference(pf.CASE_JET, vs)
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.diam, c.radius = diam, diam // 2
+    c.inflow_noise = noise
+    if noise == 1:
+        c.noise_amp = 0.05
+        c.seed = 99
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def run_pair(pf, oracle, cfg, steps, fp64=False, fields=BASIC):
+    c = cfg.copy()
+    c.storage = pf.STORAGE_FP64 if fp64 else pf.STORAGE_FP32
+    o = oracle.OracleSim(c, fp64=fp64)
+    o.step(steps)
+    with pf.Simulation(c) as s:
+        s.step(steps)
+        assert s.current_step == steps
+        errs = {f: rel_l2(s.get_field(f, dtype=np.float64), o.get_field(f)) for f in fields}
+    return errs
+
+
+CASES = [
+    ("droplet19", lambda pf: droplet_cfg(pf, 19), 120),
+    ("droplet27", lambda pf: droplet_cfg(pf, 27), 120),
+    ("jet19", lambda pf: jet_cfg(pf, 19), 80),
+    ("jet27", lambda pf: jet_cfg(pf, 27), 80),
+    ("jet19_uniform", lambda pf: jet_cfg(pf, 19, noise=1), 80),
+    ("jet27_uniform_odd", lambda pf: jet_cfg(pf, 27, nx=30, ny=34, nz=40, diam=8, noise=1), 37),
+]
+
+
+@pytest.mark.parametrize("name,make,steps", CASES, ids=[c[0] for c in CASES])
+def test_fp64_semantics(pflbm, oracle, name, make, steps):
+    errs = run_pair(pflbm, oracle, make(pflbm), steps, fp64=True, fields=ALL18)
+    bad = {k: v for k, v in errs.items() if not v <= 1e-10}
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("name,make,steps", CASES, ids=[c[0] for c in CASES])
+def test_fp32_parity(pflbm, oracle, name, make, steps):
+    errs = run_pair(pflbm, oracle, make(pflbm), steps, fp64=False, fields=ALL18)
+    bad = {k: v for k, v in errs.items() if k in BASIC and not v <= 1e-5}
+    bad.update({k: v for k, v in errs.items() if k not in BASIC and not v <= 1e-3})
+    assert not bad, errs
+
+
+@pytest.mark.parametrize("steps", [0, 1, 2, 3, 17])
+def test_step_counts_and_initial_state(pflbm, oracle, steps):
+    # odd/even counts exercise every captured graph (1, 2, 16 steps)
+    errs = run_pair(pflbm, oracle, jet_cfg(pflbm, 19, nx=24, ny=24, nz=30, diam=6), steps, fp64=True)
+    assert max(errs.values()) <= 1e-10, errs
+
+
+def test_split_stepping_equals_one_call(pflbm):
+    c = jet_cfg(pflbm, 27, nx=24, ny=24, nz=40, diam=8)
+    with pflbm.Simulation(c) as a, pflbm.Simulation(c) as b:
+        a.step(40)
+        for k in (1, 2, 16, 5, 16):
+            b.step(k)
+        for f in BASIC:
+            assert np.array_equal(a.get_field(f), b.get_field(f))
+
+
+def test_reinit_is_deterministic(pflbm):
+    c = droplet_cfg(pflbm, 19, n=24, radius=6)
+    with pflbm.Simulation(c) as s:
+        s.step(30)
+        r1 = s.get_field("phi").copy()
+        s.init()
+        s.step(30)
+        assert np.array_equal(r1, s.get_field("phi"))
+
+
+def test_phase_mass_conservation_droplet64(pflbm):
+    # the plain static droplet: phi mass conserved to 1e-6 relative over 1000 steps
+    c = pflbm.preset("droplet64")
+    with pflbm.Simulation(c) as s:
+        s.step(1)
+        m0 = s.reduce().phi_mass
+        s.step(999)
+        d = s.reduce()
+        assert d.nonfinite == 0
+        assert abs(d.phi_mass - m0) / m0 < 1e-6
+        # Laplace jump of the R=16 droplet within 35% of 2 sigma / R (diffuse interface)
+        assert d.laplace_dp == pytest.approx(2 * c.sigma / c.radius, rel=0.35)
+
+
+def test_derived_fields_match_oracle(pflbm, oracle):
+    c = jet_cfg(pflbm, 19, nx=24, ny=24, nz=36, diam=8)
+    c.flags = pflbm.FLAG_TIME_AVERAGE | pflbm.FLAG_REYNOLDS_MOMENTS | pflbm.FLAG_VORTICITY
+    c.storage = pflbm.STORAGE_FP64
+    o = oracle.OracleSim(c, fp64=True)
+    o.step(25)
+    with pflbm.Simulation(c) as s:
+        s.step(25)
+        for f in ("avg_phi", "avg_ux", "avg_uy", "avg_uz", "avg_uxux", "avg_uyuy", "avg_uzuz",
+                  "avg_uxuy", "avg_uxuz", "avg_uyuz", "vort_x", "vort_y", "vort_z", "vort_mag"):
+            assert rel_l2(s.get_field(f, dtype=np.float64), o.get_field(f)) <= 1e-10, f
+
+
+def test_low_precision_storage_close_to_fp32(pflbm):
+    c = jet_cfg(pflbm, 19, nx=32, ny=32, nz=48, diam=8)
+    ref = {}
+    with pflbm.Simulation(c) as s:
+        s.step(60)
+        ref = {f: s.get_field(f) for f in BASIC}
+    for st in (pflbm.STORAGE_FP16, pflbm.STORAGE_BF16):
+        c2 = c.copy()
+        c2.storage = st
+        with pflbm.Simulation(c2) as s:
+            s.step(60)
+            assert rel_l2(s.get_field("rho"), ref["rho"]) < 1e-4
+            assert rel_l2(s.get_field("phi"), ref["phi"]) < 2e-2
+            assert rel_l2(s.get_field("uz"), ref["uz"]) < 5e-2
+
+
+def test_write_output_layout(pflbm, tmp_path):
+    c = droplet_cfg(pflbm, 19, n=16, radius=4)
+    with pflbm.Simulation(c) as s:
+        s.step(3)
+        s.write_output(tmp_path, ("rho", "uz", "phi"))
+        n = c.nodes
+        for name in ("rho", "uz", "phi"):
+            b = tmp_path / f"{name}000002.bin"
+            assert b.stat().st_size == 4 * n
+            assert np.array_equal(np.fromfile(b, np.float32).reshape(16, 16, 16), s.get_field(name))
+        vti = (tmp_path / "step_000002.vti").read_bytes()
+        assert vti.startswith(b'<?xml version="1.0"?>')
+        assert b'WholeExtent="0 15 0 15 0 15"' in vti
+        assert b'Name="uz" NumberOfComponents="1" format="appended" offset="16388"' in vti
