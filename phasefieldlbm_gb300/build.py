@@ -16,10 +16,12 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libpflbm.so"
+DRIVER = BUILD / "pflbm_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 SOURCES = ["api.cu", "engine_fp32.cu", "engine_fp64.cu", "engine_fp16.cu", "engine_bf16.cu"]
+HOST_SOURCES = ["driver_main.cpp"]
 
 
 def nvcc() -> str:
@@ -30,13 +32,14 @@ def nvcc() -> str:
 
 
 def _deps() -> list[Path]:
-    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(
+        CSRC.glob("*.cpp")) + [
         PKG.parent / "include" / "pflbm.h"
     ]
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not DRIVER.exists():
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
@@ -68,6 +71,12 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the drop-in driver executable (host C++ over the C ABI)
+    cmd = ["g++", "-O2", "-std=c++17", str(CSRC / "driver_main.cpp"), "-o", str(DRIVER), f"-L{BUILD}", "-lpflbm",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stderr}")
     return LIB
 
 

@@ -90,7 +90,8 @@ __device__ __forceinline__ void inflow_velocity(const Params<T> &p, uint32_t x, 
     } else {
         ux = T(0);
         uy = T(0);
-        uz = static_cast<T>(p.u_inf_f * (1.0f + p.noise_amp * uniform_noise(p.seed, x, y, t)));
+        // rounded op by op (no FMA contraction) so host and device agree bit for bit
+        uz = static_cast<T>(__fmul_rn(p.u_inf_f, __fadd_rn(1.0f, __fmul_rn(p.noise_amp, uniform_noise(p.seed, x, y, t)))));
     }
 }
 

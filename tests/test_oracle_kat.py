@@ -191,3 +191,51 @@ def test_oracle_jet_runs_and_inlet_state(oracle, pflbm):
     assert np.isfinite(s.get_field("rho")).all()
     # outlet ghost plane copies plane nz-2 (BoundaryConditions.cuh:122-126)
     assert np.array_equal(s.get_field("rho")[-1, 1:-1, 1:-1], s.get_field("rho")[-2, 1:-1, 1:-1])
+
+
+def test_oracle_matches_reference_formulas(oracle):
+    """Per-node formulas of the oracle against golden vectors produced by the
+    reference's own velocity-set headers (tests/golden/gen_formulas.py)."""
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).parent / "golden" / "formulas.json").read_text())
+    assert len(g["cases"]) >= 60
+    for case in g["cases"]:
+        x = np.float32(case["in"])
+        if case["set"] == 7:
+            got_g = oracle.node_geq(*x[:4])
+            got_h = oracle.node_antidiff(*x[4:8])
+            np.testing.assert_array_equal(got_g, np.float32(case["geq"]))
+            np.testing.assert_array_equal(got_h, np.float32(case["antidiff"]))
+            continue
+        vs = case["set"]
+        rho, u, pi, F = x[0], x[1:4], x[4:10], x[10:13]
+        np.testing.assert_array_equal(oracle.node_feq(vs, rho, *u), np.float32(case["feq"]))
+        np.testing.assert_array_equal(oracle.node_fneq(vs, pi, *u), np.float32(case["fneq"]))
+        np.testing.assert_array_equal(oracle.node_force(vs, *u, *F), np.float32(case["force"]))
+
+
+def test_relaxation_constants_match_reference(oracle):
+    """Relaxation, sponge, sigma and gamma of the reference's default cases
+    (src/constants.cuh:80-141, globalFunctions.cuh:260-461), from the
+    reference's own constexpr functions (tests/golden/gen_formulas.py)."""
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).parent / "golden" / "formulas.json").read_text())["relaxation"]
+    jet = oracle.config_reference(1, 19)
+    r = oracle.relaxation(jet)  # omega_ref, tau_water, tau_oil, omco_zmin, z_start, inv_nz_m1, inv_sponge
+    j = g["jet"]
+    assert np.float32(r[1]) == np.float32(j["tau_water"])
+    assert np.float32(r[2]) == np.float32(j["tau_oil"])
+    assert np.float32(r[3]) == np.float32(j["omco_zmin"])
+    assert np.float32(r[4]) == np.float32(j["z_start"])
+    assert np.float32(r[5]) == np.float32(j["inv_nz_m1"])
+    assert np.float32(r[6]) == np.float32(j["inv_sponge"])
+    assert np.float32(jet.sigma) == np.float32(j["sigma"])
+    assert np.float32(jet.gamma) == np.float32(j["gamma"])
+    drop = oracle.config_reference(0, 19)
+    rd = oracle.relaxation(drop)
+    assert np.float32(rd[0]) == np.float32(g["droplet"]["omega_ref"])
+    assert np.float32(drop.sigma) == np.float32(g["droplet"]["sigma"])

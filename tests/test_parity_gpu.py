@@ -5,9 +5,15 @@ src/BoundaryConditions.cuh) with its single-buffer push; the library runs the
 fused two-kernel pull step. Tolerances:
   * FP64 storage vs FP64 oracle: rel. L2 <= 1e-10 on every field. Only
     summation order differs, so this pins the semantics (ghost shell, BCs,
-    step order, noise) exactly.
-  * FP32 vs FP32 oracle: rel. L2 <= 1e-5 on rho, u and phi (the tolerance of
-    the FP32 plain path), 1e-3 on the small derived quantities Pi and F.
+    step order, noise) exactly. The reference's Gaussian inflow noise is
+    computed in float with logf/cosf, whose last-ulp results differ between
+    the host libm and CUDA; jets in that mode are held to 1e-7 instead.
+  * FP32 vs FP32 oracle: rel. L2 <= 1e-5 on rho, phi and the velocity vector
+    field u (the tolerance of the FP32 plain path). Each velocity component
+    must also lie within 2x the FP32 rounding floor of the case, measured as
+    the oracle's own FP32-vs-FP64 difference (ux, uy of a young jet are pure
+    inflow noise and sit near 1e-5 in any FP32 implementation). Pi and F,
+    small differences of large terms, are held to 1e-3.
 """
 import numpy as np
 import pytest
@@ -44,7 +50,7 @@ def jet_cfg(pf, vs, nx=32, ny=32, nz=64, diam=10, noise=0, **kw):
     return c
 
 
-def run_pair(pf, oracle, cfg, steps, fp64=False, fields=BASIC):
+def run_pair(pf, oracle, cfg, steps, fp64=False, fields=BASIC, floor=False):
     c = cfg.copy()
     c.storage = pf.STORAGE_FP64 if fp64 else pf.STORAGE_FP32
     o = oracle.OracleSim(c, fp64=fp64)
@@ -52,7 +58,15 @@ def run_pair(pf, oracle, cfg, steps, fp64=False, fields=BASIC):
     with pf.Simulation(c) as s:
         s.step(steps)
         assert s.current_step == steps
-        errs = {f: rel_l2(s.get_field(f, dtype=np.float64), o.get_field(f)) for f in fields}
+        lib = {f: s.get_field(f, dtype=np.float64) for f in fields}
+    ora = {f: o.get_field(f) for f in fields}
+    errs = {f: rel_l2(lib[f], ora[f]) for f in fields}
+    if "ux" in fields:
+        errs["u"] = rel_l2(np.stack([lib[f] for f in ("ux", "uy", "uz")]), np.stack([ora[f] for f in ("ux", "uy", "uz")]))
+    if floor:
+        o64 = oracle.OracleSim(c, fp64=True)
+        o64.step(steps)
+        errs["floor"] = {f: rel_l2(ora[f], o64.get_field(f)) for f in ("rho", "ux", "uy", "uz", "phi")}
     return errs
 
 
@@ -68,23 +82,27 @@ CASES = [
 
 @pytest.mark.parametrize("name,make,steps", CASES, ids=[c[0] for c in CASES])
 def test_fp64_semantics(pflbm, oracle, name, make, steps):
-    errs = run_pair(pflbm, oracle, make(pflbm), steps, fp64=True, fields=ALL18)
-    bad = {k: v for k, v in errs.items() if not v <= 1e-10}
+    cfg = make(pflbm)
+    tol = 1e-7 if (cfg.flow_case == pflbm.CASE_JET and cfg.inflow_noise == pflbm.NOISE_GAUSSIAN_UXY) else 1e-10
+    errs = run_pair(pflbm, oracle, cfg, steps, fp64=True, fields=ALL18)
+    bad = {k: v for k, v in errs.items() if not v <= tol}
     assert not bad, bad
 
 
 @pytest.mark.parametrize("name,make,steps", CASES, ids=[c[0] for c in CASES])
 def test_fp32_parity(pflbm, oracle, name, make, steps):
-    errs = run_pair(pflbm, oracle, make(pflbm), steps, fp64=False, fields=ALL18)
-    bad = {k: v for k, v in errs.items() if k in BASIC and not v <= 1e-5}
-    bad.update({k: v for k, v in errs.items() if k not in BASIC and not v <= 1e-3})
-    assert not bad, errs
+    errs = run_pair(pflbm, oracle, make(pflbm), steps, fp64=False, fields=ALL18, floor=True)
+    floor = errs.pop("floor")
+    bad = {k: errs[k] for k in ("rho", "phi", "u") if not errs[k] <= 1e-5}
+    bad.update({k: errs[k] for k in ("ux", "uy", "uz") if not errs[k] <= max(1e-5, 2.0 * floor[k])})
+    bad.update({k: v for k, v in errs.items() if k not in BASIC + ("u",) and not v <= 1e-3})
+    assert not bad, (errs, floor)
 
 
 @pytest.mark.parametrize("steps", [0, 1, 2, 3, 17])
 def test_step_counts_and_initial_state(pflbm, oracle, steps):
     # odd/even counts exercise every captured graph (1, 2, 16 steps)
-    errs = run_pair(pflbm, oracle, jet_cfg(pflbm, 19, nx=24, ny=24, nz=30, diam=6), steps, fp64=True)
+    errs = run_pair(pflbm, oracle, jet_cfg(pflbm, 19, nx=24, ny=24, nz=30, diam=6, noise=1), steps, fp64=True)
     assert max(errs.values()) <= 1e-10, errs
 
 
@@ -109,7 +127,8 @@ def test_reinit_is_deterministic(pflbm):
 
 
 def test_phase_mass_conservation_droplet64(pflbm):
-    # the plain static droplet: phi mass conserved to 1e-6 relative over 1000 steps
+    # the plain static droplet preset (gamma = 0.05): phi mass conserved to
+    # 1e-6 relative over 1000 steps
     c = pflbm.preset("droplet64")
     with pflbm.Simulation(c) as s:
         s.step(1)
@@ -118,12 +137,24 @@ def test_phase_mass_conservation_droplet64(pflbm):
         d = s.reduce()
         assert d.nonfinite == 0
         assert abs(d.phi_mass - m0) / m0 < 1e-6
-        # Laplace jump of the R=16 droplet within 35% of 2 sigma / R (diffuse interface)
+
+
+def test_laplace_law_droplet64(pflbm):
+    # With tau_g = 1 the phase diffusivity is M = cs2/2 = 1/8, and the interface
+    # keeps the width W = 4 only for gamma = 4 M / (W cs2) = 0.5
+    # (src/constants.cuh:104-108); gamma = 0.05 relaxes to a 40-cell
+    # interface. The Laplace jump is therefore checked with gamma = 0.5:
+    # cs2 (rho_in - rho_out) within 35% of 2 sigma / R (diffuse interface).
+    c = pflbm.preset("droplet64", gamma=0.5)
+    with pflbm.Simulation(c) as s:
+        s.step(1000)
+        d = s.reduce()
+        assert d.n_in > 1000 and d.n_out > 1000
         assert d.laplace_dp == pytest.approx(2 * c.sigma / c.radius, rel=0.35)
 
 
 def test_derived_fields_match_oracle(pflbm, oracle):
-    c = jet_cfg(pflbm, 19, nx=24, ny=24, nz=36, diam=8)
+    c = jet_cfg(pflbm, 19, nx=24, ny=24, nz=36, diam=8, noise=1)
     c.flags = pflbm.FLAG_TIME_AVERAGE | pflbm.FLAG_REYNOLDS_MOMENTS | pflbm.FLAG_VORTICITY
     c.storage = pflbm.STORAGE_FP64
     o = oracle.OracleSim(c, fp64=True)
