@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import platform
 import subprocess
 from pathlib import Path
 
@@ -20,11 +21,15 @@ _LIB = None
 def build(force: bool = False) -> Path:
     src = HERE / "oracle.cpp"
     hdr = HERE.parent / "include" / "pflbm.h"
-    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= max(src.stat().st_mtime, hdr.stat().st_mtime):
+    stamp = HERE / "_build" / ".arch"
+    same_arch = stamp.exists() and stamp.read_text().strip() == platform.machine()
+    if (not force and same_arch and LIB_PATH.exists()
+            and LIB_PATH.stat().st_mtime >= max(src.stat().st_mtime, hdr.stat().st_mtime)):
         return LIB_PATH
-    r = subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], capture_output=True, text=True)
+    r = subprocess.run(["make", "-C", str(HERE), "-B"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    stamp.write_text(platform.machine())
     return LIB_PATH
 
 

@@ -19,6 +19,7 @@ TEST INFRASTRUCTURE ONLY. Two parts:
 from __future__ import annotations
 
 import json
+import platform
 import shutil
 import subprocess
 import tempfile
@@ -95,7 +96,9 @@ def build_runner() -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     exe = OUT / "ref_runner"
     src = HERE / "ref_runner.cpp"
-    if exe.exists() and exe.stat().st_mtime >= src.stat().st_mtime:
+    stamp = OUT / ".arch"
+    same_arch = stamp.exists() and stamp.read_text().strip() == platform.machine()
+    if same_arch and exe.exists() and exe.stat().st_mtime >= src.stat().st_mtime:
         return exe
     lib = CUDA / "lib64"
     stubs = lib / "stubs"
@@ -104,6 +107,7 @@ def build_runner() -> Path:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("ref_runner build failed:\n" + r.stderr)
+    stamp.write_text(platform.machine())
     return exe
 
 

@@ -7,6 +7,7 @@ population storage type, then linked with ``nvcc -shared``.
 from __future__ import annotations
 
 import os
+import platform
 import shutil
 import subprocess
 from concurrent.futures import ThreadPoolExecutor
@@ -38,8 +39,14 @@ def _deps() -> list[Path]:
     ]
 
 
+STAMP = BUILD / ".arch"
+
+
 def up_to_date() -> bool:
     if not LIB.exists() or not DRIVER.exists():
+        return False
+    # binaries built on another architecture are never reused
+    if not STAMP.exists() or STAMP.read_text().strip() != platform.machine():
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
@@ -77,6 +84,7 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    STAMP.write_text(platform.machine())
     return LIB
 
 
