@@ -245,7 +245,23 @@ def run_gpu(args, ranks: Ranks) -> dict:
                "per_step": f"{inner} lattice steps + upload of the initial rho,u,phi + readback of rho,uz,phi"}
     except Exception as ex:  # the CUDA path must not fall back; report why e2e is missing
         e2e = {"value": None, "unit": "MLUPS", "error": str(ex)[:200]}
+    tma = sim.uses_tma
     sim.close()
+
+    # other lattices / storage precisions on the same jet (informational)
+    variants = {}
+    if not args.no_variants:
+        for name, wl, st in (("jet_d3q19_fp32", "jet_d3q19", pf.STORAGE_FP32),
+                             ("jet_d3q19_fp16", "jet_d3q19", pf.STORAGE_FP16),
+                             ("jet_d3q19_bf16", "jet_d3q19", pf.STORAGE_BF16),
+                             ("jet_d3q27_fp16", "jet_d3q27", pf.STORAGE_FP16)):
+            c2 = pf.preset(wl, storage=st, device=cfg.device)
+            with pf.Simulation(c2) as s2:
+                s2.step(3 * inner // 2)
+                s2.synchronize()
+                tot2, k2 = s2.step_profiled(2 * inner)
+                variants[name] = {"mlups": round(c2.nodes * 2 * inner / (tot2 / 1e3) / 1e6, 1),
+                                  "collide_ms": round(k2[0] / (2 * inner), 4), "phase_ms": round(k2[1] / (2 * inner), 4)}
 
     cpu = None
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
@@ -266,7 +282,8 @@ def run_gpu(args, ranks: Ranks) -> dict:
                    "l2": "inputs larger than L2 (f ping-pong 2x{:.0f} MB)".format(q * s_f * N / 1e6),
                    "parallelism": f"replicas x{ranks.world}"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": 2 * lattice_steps, "clocks": clk, "diverged": diverged,
+        "gpu_launches": 2 * lattice_steps, "clocks": clk, "diverged": diverged, "tma": tma,
+        "variants": variants,
     }
 
 
@@ -306,6 +323,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="jet_d3q27")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

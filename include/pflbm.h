@@ -197,13 +197,47 @@ int pflbm_reduce(pflbm_sim *sim, pflbm_diag *out);
  * that appends them (src/postProcess/PostProcess.cuh:43-261). */
 int pflbm_write_output(pflbm_sim *sim, const char *dir, const int32_t *field_ids, int32_t n_fields);
 
+/* Checkpoint and resume (the reference has none; its .bin dumps are
+ * output only, src/main.cu:130-133). The file holds the configuration, the
+ * step count, both ping-pong population and phi buffers (ghost values
+ * included) and the derived averages. Loading requires the same grid, lattice, case
+ * and storage; the run then continues bit for bit as if uninterrupted. */
+int pflbm_save_checkpoint(pflbm_sim *sim, const char *path);
+int pflbm_load_checkpoint(pflbm_sim *sim, const char *path);
+
 /* Device bytes held by the simulation. */
 int pflbm_device_bytes(const pflbm_sim *sim, uint64_t *bytes);
+
+/* 1 when the collide kernel is fed by TMA bulk tensor copies (needs
+ * 16-byte aligned rows: nx*element size % 16 == 0), 0 for plain loads. */
+int pflbm_uses_tma(const pflbm_sim *sim, int32_t *flag);
 
 /* Number of CUDA kernels one time step launches (launch accounting). */
 int pflbm_kernels_per_step(const pflbm_sim *sim, int32_t *count);
 
 int pflbm_destroy(pflbm_sim *sim);
+
+/* ---- batched ensembles (no counterpart in the reference) ---------------
+ * Many independent periodic droplet boxes (FP32, one velocity set, possibly
+ * different sizes and physics) advance together: every step is two
+ * persistent kernel launches covering all boxes through a device work list,
+ * captured in CUDA graphs. Fields and diagnostics are per box and mean the
+ * same as for a single simulation. */
+typedef struct pflbm_ensemble pflbm_ensemble;
+int pflbm_ensemble_create(const pflbm_config *cfgs, int32_t n_boxes, pflbm_ensemble **out);
+int pflbm_ensemble_init(pflbm_ensemble *ens);
+int pflbm_ensemble_step(pflbm_ensemble *ens, uint64_t nsteps);
+int pflbm_ensemble_step_profiled(pflbm_ensemble *ens, uint64_t nsteps, double *ms);
+int pflbm_ensemble_get_field(pflbm_ensemble *ens, int32_t box, int32_t field_id, void *host_dst, size_t bytes);
+int pflbm_ensemble_reduce(pflbm_ensemble *ens, int32_t box, pflbm_diag *out);
+/* Work granularity: z planes per work item, resident CTAs per SM (1 or 2). */
+int pflbm_ensemble_set_tuning(pflbm_ensemble *ens, int32_t zchunk, int32_t ctas_per_sm);
+/* Measured autotuner: times each candidate tuning for trial_steps steps,
+ * keeps the fastest and re-initialises the ensemble. */
+int pflbm_ensemble_autotune(pflbm_ensemble *ens, int32_t trial_steps, int32_t *best_zchunk, int32_t *best_ctas,
+                            double *best_ms);
+int pflbm_ensemble_info(const pflbm_ensemble *ens, uint64_t *total_nodes, int32_t *n_boxes, int32_t *n_items);
+int pflbm_ensemble_destroy(pflbm_ensemble *ens);
 
 #ifdef __cplusplus
 }

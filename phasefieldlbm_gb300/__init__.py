@@ -23,7 +23,7 @@ __all__ = [
     "NOISE_GAUSSIAN_UXY", "NOISE_UNIFORM_UZ",
     "FLAG_TIME_AVERAGE", "FLAG_REYNOLDS_MOMENTS", "FLAG_VORTICITY",
     "FIELDS", "Config", "Diag", "PflbmError", "Simulation",
-    "load_library", "config_reference", "preset", "EXPORTED_SYMBOLS",
+    "load_library", "config_reference", "preset", "EXPORTED_SYMBOLS", "Ensemble", "ensemble_configs",
 ]
 
 CASE_DROPLET, CASE_JET = 0, 1
@@ -46,8 +46,12 @@ EXPORTED_SYMBOLS = [
     "pflbm_abi_version", "pflbm_last_error", "pflbm_config_reference", "pflbm_create",
     "pflbm_init", "pflbm_set_initial_field", "pflbm_step", "pflbm_step_async",
     "pflbm_synchronize", "pflbm_step_profiled", "pflbm_current_step", "pflbm_get_field", "pflbm_get_field_f64",
-    "pflbm_reduce", "pflbm_write_output", "pflbm_device_bytes", "pflbm_kernels_per_step",
+    "pflbm_reduce", "pflbm_write_output", "pflbm_save_checkpoint", "pflbm_load_checkpoint",
+    "pflbm_device_bytes", "pflbm_uses_tma", "pflbm_kernels_per_step",
     "pflbm_destroy",
+    "pflbm_ensemble_create", "pflbm_ensemble_init", "pflbm_ensemble_step", "pflbm_ensemble_step_profiled",
+    "pflbm_ensemble_get_field", "pflbm_ensemble_reduce", "pflbm_ensemble_set_tuning", "pflbm_ensemble_autotune",
+    "pflbm_ensemble_info", "pflbm_ensemble_destroy",
 ]
 
 
@@ -157,8 +161,22 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_reduce": ([vp, ctypes.POINTER(Diag)], ctypes.c_int),
         "pflbm_write_output": ([vp, ctypes.c_char_p, ctypes.POINTER(i32), i32], ctypes.c_int),
         "pflbm_device_bytes": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
+        "pflbm_save_checkpoint": ([vp, ctypes.c_char_p], ctypes.c_int),
+        "pflbm_load_checkpoint": ([vp, ctypes.c_char_p], ctypes.c_int),
         "pflbm_kernels_per_step": ([vp, ctypes.POINTER(i32)], ctypes.c_int),
+        "pflbm_uses_tma": ([vp, ctypes.POINTER(i32)], ctypes.c_int),
         "pflbm_destroy": ([vp], ctypes.c_int),
+        "pflbm_ensemble_create": ([ctypes.POINTER(Config), i32, ctypes.POINTER(vp)], ctypes.c_int),
+        "pflbm_ensemble_init": ([vp], ctypes.c_int),
+        "pflbm_ensemble_step": ([vp, u64], ctypes.c_int),
+        "pflbm_ensemble_step_profiled": ([vp, u64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "pflbm_ensemble_get_field": ([vp, i32, i32, vp, sz], ctypes.c_int),
+        "pflbm_ensemble_reduce": ([vp, i32, ctypes.POINTER(Diag)], ctypes.c_int),
+        "pflbm_ensemble_set_tuning": ([vp, i32, i32], ctypes.c_int),
+        "pflbm_ensemble_autotune": ([vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double)],
+                                    ctypes.c_int),
+        "pflbm_ensemble_info": ([vp, ctypes.POINTER(u64), ctypes.POINTER(i32), ctypes.POINTER(i32)], ctypes.c_int),
+        "pflbm_ensemble_destroy": ([vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -235,6 +253,104 @@ def preset(name: str, **overrides) -> Config:
         else:
             setattr(c, k, v)
     return c
+
+
+def ensemble_configs(n: int = 64, seed: int = 2026, velocity_set: int = VS_D3Q19) -> list:
+    """The seeded droplet ensemble: edges uniform in {32,48,64,80,96}, radius
+    uniform in 15-30% of the edge, centre offset uniform within +-10%, sigma
+    log-uniform in [1e-3, 1e-2], tau uniform in [0.55, 0.9], initial velocity
+    seeded uniform +-1e-3, spherical droplets, D3Q19 + D3Q7, FP32."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        c = config_reference(CASE_DROPLET, velocity_set)
+        e = int(rng.choice([32, 48, 64, 80, 96]))
+        c.nx = c.ny = c.nz = e
+        c.radius = max(2, int(round(rng.uniform(0.15, 0.30) * e)))
+        c.diam = 2 * c.radius
+        off = rng.uniform(-0.1, 0.1, 3) * e
+        for i in range(3):
+            c.center_offset[i] = float(off[i])
+        c.sigma = float(10 ** rng.uniform(-3, -2))
+        c.tau = float(rng.uniform(0.55, 0.9))
+        c.droplet_x_stretch = 1.0
+        c.init_noise = 1e-3
+        c.seed = int(seed * 1000 + k)
+        out.append(c)
+    return out
+
+
+class Ensemble:
+    """A batch of droplet boxes advanced together (pflbm_ensemble_*)."""
+
+    def __init__(self, configs, init: bool = True):
+        self.lib = load_library()
+        arr = (Config * len(configs))()
+        for i, c in enumerate(configs):
+            ctypes.memmove(ctypes.byref(arr[i]), ctypes.byref(c), ctypes.sizeof(Config))
+            arr[i].struct_size = ctypes.sizeof(Config)
+        self.configs = [c.copy() for c in configs]
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.pflbm_ensemble_create(arr, len(configs), ctypes.byref(h)))
+        self._h = h
+        if init:
+            self.init()
+
+    def init(self):
+        _check(self.lib, self.lib.pflbm_ensemble_init(self._h))
+
+    def step(self, n: int = 1):
+        _check(self.lib, self.lib.pflbm_ensemble_step(self._h, int(n)))
+
+    def step_profiled(self, n: int) -> float:
+        ms = ctypes.c_double()
+        _check(self.lib, self.lib.pflbm_ensemble_step_profiled(self._h, int(n), ctypes.byref(ms)))
+        return float(ms.value)
+
+    def get_field(self, box: int, name: str) -> np.ndarray:
+        c = self.configs[box]
+        a = np.empty((int(c.nz), int(c.ny), int(c.nx)), np.float32)
+        _check(self.lib, self.lib.pflbm_ensemble_get_field(self._h, box, FIELD_ID[name], a.ctypes.data, a.nbytes))
+        return a
+
+    def reduce(self, box: int) -> Diag:
+        d = Diag()
+        rc = self.lib.pflbm_ensemble_reduce(self._h, box, ctypes.byref(d))
+        if rc not in (0, 5):
+            _check(self.lib, rc)
+        return d
+
+    def set_tuning(self, zchunk: int, ctas_per_sm: int):
+        _check(self.lib, self.lib.pflbm_ensemble_set_tuning(self._h, zchunk, ctas_per_sm))
+
+    def autotune(self, trial_steps: int = 10) -> dict:
+        z, c, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+        _check(self.lib, self.lib.pflbm_ensemble_autotune(self._h, trial_steps, ctypes.byref(z), ctypes.byref(c),
+                                                          ctypes.byref(ms)))
+        return {"zchunk": z.value, "ctas_per_sm": c.value, "trial_ms": ms.value}
+
+    @property
+    def info(self) -> dict:
+        n, b, it = ctypes.c_uint64(), ctypes.c_int32(), ctypes.c_int32()
+        _check(self.lib, self.lib.pflbm_ensemble_info(self._h, ctypes.byref(n), ctypes.byref(b), ctypes.byref(it)))
+        return {"nodes": n.value, "boxes": b.value, "work_items": it.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.pflbm_ensemble_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Simulation:
@@ -323,11 +439,23 @@ class Simulation:
         ids = (ctypes.c_int32 * len(fields))(*[FIELD_ID[f] for f in fields])
         _check(self.lib, self.lib.pflbm_write_output(self._h, str(directory).encode(), ids, len(fields)))
 
+    def save_checkpoint(self, path):
+        _check(self.lib, self.lib.pflbm_save_checkpoint(self._h, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        _check(self.lib, self.lib.pflbm_load_checkpoint(self._h, str(path).encode()))
+
     @property
     def device_bytes(self) -> int:
         v = ctypes.c_uint64()
         _check(self.lib, self.lib.pflbm_device_bytes(self._h, ctypes.byref(v)))
         return int(v.value)
+
+    @property
+    def uses_tma(self) -> bool:
+        v = ctypes.c_int32()
+        _check(self.lib, self.lib.pflbm_uses_tma(self._h, ctypes.byref(v)))
+        return bool(v.value)
 
     @property
     def kernels_per_step(self) -> int:

@@ -8,6 +8,7 @@
 // launches and no host synchronisation until the caller asks for one.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -65,7 +66,7 @@ struct pflbm_sim {
     double *dev_diag = nullptr;
 };
 
-namespace {
+namespace pflbm {
 
 // Derived constants as the reference computes them
 // (src/constants.cuh:80-141, src/functions/globalFunctions.cuh:104-461).
@@ -159,6 +160,14 @@ int validate(const pflbm_config &c) {
     return PFLBM_OK;
 }
 
+void set_error(const std::string &msg) { g_err = msg; }
+
+}  // namespace pflbm
+
+namespace {
+using pflbm::derive;
+using pflbm::validate;
+
 int pick_zchunk(const pflbm_config &c, int device) {
     if (const char *e = std::getenv("PFLBM_ZCHUNK")) {
         const int v = std::atoi(e);
@@ -202,6 +211,15 @@ int capture(pflbm_sim *s, int parity, int nsteps, cudaGraphExec_t *out) {
     return PFLBM_OK;
 }
 
+// Reads the device error word (set by a kernel whose bounded wait gave up).
+int check_device_error(pflbm_sim *s) {
+    unsigned int w = 0;
+    cudaError_t e = cudaMemcpy(&w, s->eng->error_word(), sizeof w, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "error word readback");
+    if (w != 0) return fail(PFLBM_ERR_DEVICE, "a kernel gave up waiting for its TMA copies (error word " + std::to_string(w) + ")");
+    return PFLBM_OK;
+}
+
 // Rebuilds f and phi from the initial fields after pflbm_set_initial_field.
 void flush_initial(pflbm_sim *s) {
     if (s->distros_dirty) {
@@ -212,7 +230,7 @@ void flush_initial(pflbm_sim *s) {
 
 int ensure_cache(pflbm_sim *s) {
     if (s->cache_step == int64_t(s->step)) return PFLBM_OK;
-    if (s->step == 0) {
+    if (s->step == 0 && s->cache_step == 0) {
         // the cache still holds the initial fields
         s->cache_step = 0;
         return PFLBM_OK;
@@ -473,7 +491,7 @@ int pflbm_synchronize(pflbm_sim *s) {
     if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-    return PFLBM_OK;
+    return check_device_error(s);
 }
 
 int pflbm_step(pflbm_sim *s, uint64_t n) {
@@ -517,7 +535,7 @@ int pflbm_step_profiled(pflbm_sim *s, uint64_t n, double *total_ms, double *kern
     for (auto &x : ev) cudaEventDestroy(x);
     if (e != cudaSuccess) return cuda_fail(e, "pflbm_step_profiled");
     for (int k = 0; k < nk; ++k) kernel_ms[k] = k < 2 ? sums[k] : 0.0;
-    return PFLBM_OK;
+    return check_device_error(s);
 }
 
 int pflbm_current_step(const pflbm_sim *s, uint64_t *step) {
@@ -626,9 +644,115 @@ int pflbm_write_output(pflbm_sim *s, const char *dir, const int32_t *ids, int32_
     return PFLBM_OK;
 }
 
+// Checkpoint file: header, both ping-pong population buffers (the one the
+// next step reads first), both phi buffers (ghost values included), the
+// derived averages when enabled. Both buffers are kept so that the slots no
+// step rewrites and the readback of the last completed step stay exact.
+namespace {
+struct CkptHeader {
+    char magic[8];        // "PFLBMCK1"
+    uint32_t abi;
+    uint32_t header_bytes;
+    pflbm_config cfg;
+    uint64_t step;
+    uint64_t f_bytes, phi_bytes, avg_bytes;
+};
+
+int write_blob(std::ofstream &o, const void *dev, uint64_t bytes) {
+    std::vector<char> h(1 << 26);
+    for (uint64_t off = 0; off < bytes; off += h.size()) {
+        const size_t n = size_t(std::min<uint64_t>(h.size(), bytes - off));
+        cudaError_t e = cudaMemcpy(h.data(), static_cast<const char *>(dev) + off, n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "checkpoint D2H");
+        o.write(h.data(), std::streamsize(n));
+        if (!o) return fail(PFLBM_ERR_IO, "checkpoint write failed");
+    }
+    return PFLBM_OK;
+}
+
+int read_blob(std::ifstream &in, void *dev0, void *dev1, uint64_t bytes) {
+    std::vector<char> h(1 << 26);
+    for (uint64_t off = 0; off < bytes; off += h.size()) {
+        const size_t n = size_t(std::min<uint64_t>(h.size(), bytes - off));
+        in.read(h.data(), std::streamsize(n));
+        if (!in) return fail(PFLBM_ERR_IO, "checkpoint truncated");
+        for (void *d : {dev0, dev1}) {
+            if (!d) continue;
+            cudaError_t e = cudaMemcpy(static_cast<char *>(d) + off, h.data(), n, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cuda_fail(e, "checkpoint H2D");
+        }
+    }
+    return PFLBM_OK;
+}
+}  // namespace
+
+int pflbm_save_checkpoint(pflbm_sim *s, const char *path) {
+    if (!s || !path) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
+    if (!s->initialized) return fail(PFLBM_ERR_STATE, "pflbm_init has not been called");
+    cudaSetDevice(s->device);
+    flush_initial(s);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "checkpoint sync");
+    CkptHeader h{};
+    std::memcpy(h.magic, "PFLBMCK1", 8);
+    h.abi = PFLBM_ABI_VERSION;
+    h.header_bytes = sizeof(CkptHeader);
+    h.cfg = s->cfg;
+    h.step = s->step;
+    h.f_bytes = s->eng->f_bytes();
+    h.phi_bytes = s->eng->phi_bytes();
+    h.avg_bytes = s->eng->avg_bytes();
+    std::ofstream o(path, std::ios::binary | std::ios::trunc);
+    if (!o) return fail(PFLBM_ERR_IO, std::string("cannot open ") + path);
+    o.write(reinterpret_cast<const char *>(&h), sizeof h);
+    int rc = write_blob(o, s->eng->f_ptr(s->parity), h.f_bytes);
+    if (!rc) rc = write_blob(o, s->eng->f_ptr(s->parity ^ 1), h.f_bytes);
+    if (!rc) rc = write_blob(o, s->eng->phi_ptr(s->parity), h.phi_bytes);
+    if (!rc) rc = write_blob(o, s->eng->phi_ptr(s->parity ^ 1), h.phi_bytes);
+    if (!rc && h.avg_bytes) rc = write_blob(o, s->eng->avg_ptr(), h.avg_bytes);
+    return rc;
+}
+
+int pflbm_load_checkpoint(pflbm_sim *s, const char *path) {
+    if (!s || !path) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
+    cudaSetDevice(s->device);
+    std::ifstream in(path, std::ios::binary);
+    if (!in) return fail(PFLBM_ERR_IO, std::string("cannot open ") + path);
+    CkptHeader h{};
+    in.read(reinterpret_cast<char *>(&h), sizeof h);
+    if (!in || std::memcmp(h.magic, "PFLBMCK1", 8) != 0 || h.header_bytes != sizeof(CkptHeader))
+        return fail(PFLBM_ERR_IO, "not a pflbm checkpoint");
+    const pflbm_config &a = h.cfg, &b = s->cfg;
+    if (a.nx != b.nx || a.ny != b.ny || a.nz != b.nz || a.velocity_set != b.velocity_set ||
+        a.flow_case != b.flow_case || a.storage != b.storage || h.f_bytes != s->eng->f_bytes() ||
+        h.phi_bytes != s->eng->phi_bytes() || h.avg_bytes != s->eng->avg_bytes())
+        return fail(PFLBM_ERR_INVALID_ARG, "checkpoint does not match this simulation's grid, lattice or storage");
+    cudaStreamSynchronize(s->stream);
+    int rc = read_blob(in, s->eng->f_ptr(0), nullptr, h.f_bytes);
+    if (!rc) rc = read_blob(in, s->eng->f_ptr(1), nullptr, h.f_bytes);
+    if (!rc) rc = read_blob(in, s->eng->phi_ptr(0), nullptr, h.phi_bytes);
+    if (!rc) rc = read_blob(in, s->eng->phi_ptr(1), nullptr, h.phi_bytes);
+    if (!rc && h.avg_bytes) rc = read_blob(in, s->eng->avg_ptr(), nullptr, h.avg_bytes);
+    if (rc) return rc;
+    s->eng->reset_counters(s->stream);
+    s->eng->set_counter(0, h.step, s->stream);
+    s->parity = 0;
+    s->step = h.step;
+    s->cache_step = -1;
+    s->distros_dirty = false;
+    s->initialized = true;
+    return PFLBM_OK;
+}
+
 int pflbm_device_bytes(const pflbm_sim *s, uint64_t *bytes) {
     if (!s || !bytes) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
     *bytes = s->eng->device_bytes();
+    return PFLBM_OK;
+}
+
+int pflbm_uses_tma(const pflbm_sim *s, int32_t *flag) {
+    if (!s || !flag) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
+    *flag = s->eng->uses_tma() ? 1 : 0;
     return PFLBM_OK;
 }
 

@@ -57,8 +57,24 @@ class Engine {
     virtual void *avg_ptr() = 0;    // 10*N reals or null
     virtual void *vort_ptr() = 0;   // 4*N reals or null
     virtual uint64_t device_bytes() const = 0;
+    // Raw state buffers for checkpoints.
+    virtual void *f_ptr(int k) = 0;
+    virtual void *phi_ptr(int k) = 0;
+    virtual uint64_t f_bytes() const = 0;
+    virtual uint64_t phi_bytes() const = 0;
+    virtual uint64_t avg_bytes() const = 0;
+    virtual void set_counter(int parity, unsigned long long value, cudaStream_t s) = 0;
+    // Device word that kernels set when a bounded wait gave up (0 = fine).
+    virtual unsigned int *error_word() = 0;
+    // True when the TMA-fed collide kernel is in use.
+    virtual bool uses_tma() const = 0;
     virtual int kernels_per_step() const = 0;
 };
+
+// api.cu: derived constants, validation and the thread-local error message.
+void derive(const pflbm_config &c, HostParams &h);
+int validate(const pflbm_config &c);
+void set_error(const std::string &msg);
 
 Engine *make_engine_fp32(int q, bool jet, const HostParams &hp, uint32_t flags);
 Engine *make_engine_fp64(int q, bool jet, const HostParams &hp, uint32_t flags);

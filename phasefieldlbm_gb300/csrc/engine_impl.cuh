@@ -5,8 +5,12 @@
 #include <cstring>
 #include <new>
 
+#include <cstdlib>
+#include <type_traits>
+
 #include "engine.h"
 #include "kernels.cuh"
+#include "kernels_tma.cuh"
 
 namespace pflbm {
 
@@ -68,6 +72,7 @@ class EngineT final : public Engine {
             {reinterpret_cast<void **>(&top_), sizeof(T) * 22 * plane},
             {reinterpret_cast<void **>(&macro_), sizeof(T) * M_COUNT * N},
             {reinterpret_cast<void **>(&counters_), sizeof(unsigned long long) * 2},
+            {reinterpret_cast<void **>(&err_), sizeof(unsigned int) * 4},
             {reinterpret_cast<void **>(&partial_), sizeof(double) * RED_FIELDS * kRedBlocks},
         };
         for (auto &r : reqs) {
@@ -104,11 +109,66 @@ class EngineT final : public Engine {
             err = cudaGetErrorString(cudaGetLastError());
             return PFLBM_ERR_CUDA;
         }
+        setup_tma();
         return PFLBM_OK;
     }
 
+    // The TMA collide kernel needs 16-byte aligned row strides; otherwise the
+    // plain-load kernel is used. PFLBM_NO_TMA=1 forces the plain kernel.
+    void setup_tma() {
+        use_tma_ = false;
+        if (const char *e = std::getenv("PFLBM_NO_VEC")) no_vec_ = e[0] == '1';
+        if (const char *e = std::getenv("PFLBM_NO_TMA"))
+            if (e[0] == '1') return;
+        if ((uint64_t(h_.nx) * sizeof(S)) % 16 != 0 || (uint64_t(h_.nx) * sizeof(T)) % 16 != 0) return;
+        using L = TmaLayout<QQ, S>;
+        using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return;
+        }
+        Encode enc = reinterpret_cast<Encode>(fn);
+        CUtensorMapDataType ft = std::is_same<S, float>::value    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                 : std::is_same<S, double>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                 : std::is_same<S, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+        CUtensorMapDataType pt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        const uint64_t nx = h_.nx, ny = h_.ny, nz = h_.nz, N = h_.N;
+        for (int k = 0; k < 2; ++k) {
+            const cuuint64_t fdim[4] = {nx, ny, nz, cuuint64_t(QQ)};
+            const cuuint64_t fstr[3] = {nx * sizeof(S), nx * ny * sizeof(S), N * sizeof(S)};
+            const cuuint32_t fbox[4] = {cuuint32_t(L::BW), cuuint32_t(TY), 1, 1};
+            const cuuint32_t one4[4] = {1, 1, 1, 1};
+            if (enc(&fmap_[k], ft, 4, f_[k], fdim, fstr, fbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return;
+            const cuuint64_t pdim[3] = {nx, ny, nz};
+            const cuuint64_t pstr[2] = {nx * sizeof(T), nx * ny * sizeof(T)};
+            const cuuint32_t pbox[3] = {cuuint32_t(L::PBW), cuuint32_t(L::PBH), 1};
+            if (enc(&phimap_[k], pt, 3, phi_[k], pdim, pstr, pbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return;
+        }
+        if (cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(L::total)) != cudaSuccess ||
+            cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_AVG>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(L::total)) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        use_tma_ = true;
+    }
+
     void free_all() override {
-        void *ptrs[] = {f_[0], f_[1], phi_[0], phi_[1], j_, top_, macro_, counters_, partial_, avg_, vort_};
+        void *ptrs[] = {f_[0], f_[1], phi_[0], phi_[1], j_, top_, macro_, counters_, partial_, avg_, vort_, err_};
         for (void *q : ptrs)
             if (q) cudaFree(q);
         f_[0] = f_[1] = nullptr;
@@ -116,6 +176,7 @@ class EngineT final : public Engine {
         j_ = top_ = macro_ = avg_ = vort_ = nullptr;
         counters_ = nullptr;
         partial_ = nullptr;
+        err_ = nullptr;
         bytes_ = 0;
     }
 
@@ -132,7 +193,7 @@ class EngineT final : public Engine {
         b.t_fixed = 0;
         b.avg = avg_;
         b.macro = macro_;
-        b.err = nullptr;
+        b.err = err_;
         return b;
     }
 
@@ -147,13 +208,31 @@ class EngineT final : public Engine {
     void enqueue_step(int parity, cudaStream_t s, cudaEvent_t *ev) override {
         const StepBuffers<S, T> b = buffers(parity);
         if (ev) cudaEventRecord(ev[0], s);
-        if (avg_)
+        if (use_tma_) {
+            const size_t sm = TmaLayout<QQ, S>::total;
+            if (avg_)
+                k_collide_tma<QQ, JET, S, MODE_STEP_AVG>
+                    <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+            else
+                k_collide_tma<QQ, JET, S, MODE_STEP>
+                    <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+        } else if (avg_) {
             k_collide<QQ, JET, S, MODE_STEP_AVG><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
-        else
+        } else {
             k_collide<QQ, JET, S, MODE_STEP><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
+        }
         if (ev) cudaEventRecord(ev[1], s);
         if (ev) cudaEventRecord(ev[2], s);
-        k_phase<QQ, JET, S><<<node_grid(), node_block(), 0, s>>>(p_, b);
+        if constexpr (std::is_same<T, float>::value) {
+            if (h_.nx % 4 == 0 && !no_vec_) {
+                const dim3 g4((h_.nx / 4 + 31) / 32, (h_.ny + 7) / 8, h_.nz);
+                k_phase_v4<QQ, JET, S><<<g4, node_block(), 0, s>>>(p_, b);
+            } else {
+                k_phase<QQ, JET, S><<<node_grid(), node_block(), 0, s>>>(p_, b);
+            }
+        } else {
+            k_phase<QQ, JET, S><<<node_grid(), node_block(), 0, s>>>(p_, b);
+        }
         if (ev) cudaEventRecord(ev[3], s);
     }
 
@@ -195,7 +274,19 @@ class EngineT final : public Engine {
     }
     void reset_counters(cudaStream_t s) override {
         cudaMemsetAsync(counters_, 0, sizeof(unsigned long long) * 2, s);
+        cudaMemsetAsync(err_, 0, sizeof(unsigned int) * 4, s);
     }
+    unsigned int *error_word() override { return err_; }
+    void *f_ptr(int k) override { return f_[k]; }
+    void *phi_ptr(int k) override { return phi_[k]; }
+    uint64_t f_bytes() const override { return sizeof(S) * QQ * h_.N; }
+    uint64_t phi_bytes() const override { return sizeof(T) * h_.N; }
+    uint64_t avg_bytes() const override { return avg_ ? sizeof(T) * 10 * h_.N : 0; }
+    void set_counter(int parity, unsigned long long value, cudaStream_t s) override {
+        cudaMemcpyAsync(counters_ + parity, &value, sizeof value, cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+    }
+    bool uses_tma() const override { return use_tma_; }
     int real_bytes() const override { return int(sizeof(T)); }
     void *macro_ptr() override { return macro_; }
     void *avg_ptr() override { return avg_; }
@@ -213,6 +304,10 @@ class EngineT final : public Engine {
     T *j_ = nullptr, *top_ = nullptr, *macro_ = nullptr, *avg_ = nullptr, *vort_ = nullptr;
     unsigned long long *counters_ = nullptr;
     double *partial_ = nullptr;
+    unsigned int *err_ = nullptr;
+    bool use_tma_ = false;
+    bool no_vec_ = false;  // PFLBM_NO_VEC=1: scalar phase kernel
+    CUtensorMap fmap_[2]{}, phimap_[2]{};
     uint64_t bytes_ = 0;
 };
 

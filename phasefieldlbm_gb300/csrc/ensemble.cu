@@ -1,0 +1,504 @@
+// ensemble.cu - batched ensembles of independent periodic droplet boxes.
+//
+// Extension of the hot path (no counterpart in the reference, whose grid is
+// fixed at compile time): many boxes of different sizes advance together.
+// All boxes live in shared allocations (per-box offsets). One time step is
+// two persistent launches covering every box: a fixed grid of CTAs pulls
+// work items (box, 32x8 column tile, z chunk) from a device counter and runs
+// the same tile code as the single-box collide and phase kernels. Chunks of
+// steps are captured into CUDA graphs. The z-chunk length and the number of
+// resident CTAs per SM are chosen by a measured autotuner.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/pflbm.h"
+#include "engine_impl.cuh"
+
+namespace pflbm {
+
+struct BoxDev {
+    Params<float> p;
+    uint64_t f_off;  // element offset of the box's Q*N block in the f buffers
+    uint64_t n_off;  // element offset of the box's N block in node arrays
+};
+
+struct WorkItem {
+    int box, x0, y0, zb, ze;
+};
+
+struct BatchPtrs {
+    float *f[2];
+    float *phi[2];
+    float *J;
+    unsigned long long *step;  // [2] ping-pong step counters
+    unsigned int *ctr;         // [2] work counters (collide, phase)
+    unsigned int *err;
+};
+
+__device__ __forceinline__ StepBuffers<float, float> box_buffers(const BatchPtrs &bp, const BoxDev &bx, int parity) {
+    StepBuffers<float, float> b{};
+    b.f_src = bp.f[parity] + bx.f_off;
+    b.f_dst = bp.f[parity ^ 1] + bx.f_off;
+    b.phi_src = bp.phi[parity] + bx.n_off;
+    b.phi_dst = bp.phi[parity ^ 1] + bx.n_off;
+    b.jflux = bp.J + 3 * bx.n_off;
+    b.top = nullptr;
+    b.step_in = bp.step + parity;
+    b.step_out = bp.step + (parity ^ 1);
+    b.t_fixed = 0;
+    b.avg = nullptr;
+    b.macro = nullptr;
+    b.err = bp.err;
+    return b;
+}
+
+// Persistent collide over all boxes. Resets the phase kernel's counter (the
+// previous phase launch has finished; the next one starts after this one).
+template <int QQ>
+__global__ void __launch_bounds__(NT, 2)
+    k_collide_batch(const BoxDev *boxes, const WorkItem *items, int n_items, BatchPtrs bp, int parity) {
+    __shared__ CollideSmem<float> sm;
+    __shared__ int s_item;
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    if (blockIdx.x == 0 && tid == 0) bp.ctr[1] = 0u;
+    for (;;) {
+        if (tid == 0) s_item = int(atomicAdd(&bp.ctr[0], 1u));
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const WorkItem w = items[it];
+        const BoxDev &bx = boxes[w.box];
+        const StepBuffers<float, float> b = box_buffers(bp, bx, parity);
+        collide_tile<QQ, false, float, MODE_STEP>(bx.p, b, w.x0, w.y0, w.zb, w.ze, sm);
+        __syncthreads();  // shared rings are reused by the next item
+    }
+}
+
+// Persistent phase step over the same work items; advances the step counter
+// and resets the collide kernel's work counter.
+template <int QQ>
+__global__ void __launch_bounds__(NT)
+    k_phase_batch(const BoxDev *boxes, const WorkItem *items, int n_items, BatchPtrs bp, int parity) {
+    __shared__ int s_item;
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    const uint32_t t = static_cast<uint32_t>(bp.step[parity]);
+    if (blockIdx.x == 0 && tid == 0) {
+        bp.ctr[0] = 0u;
+        bp.step[parity ^ 1] = bp.step[parity] + 1ull;
+    }
+    for (;;) {
+        if (tid == 0) s_item = int(atomicAdd(&bp.ctr[1], 1u));
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const WorkItem w = items[it];
+        const BoxDev &bx = boxes[w.box];
+        const StepBuffers<float, float> b = box_buffers(bp, bx, parity);
+        const int x = w.x0 + int(threadIdx.x), y = w.y0 + int(threadIdx.y);
+        if (x >= 1 && x <= int(bx.p.nx) - 2 && y >= 1 && y <= int(bx.p.ny) - 2)
+            for (int z = w.zb; z < w.ze; ++z) phase_node<QQ, false, float>(bx.p, b, x, y, z, t);
+    }
+}
+
+class Ensemble {
+   public:
+    int q = 19;
+    int device = 0;
+    int sms = 152;
+    std::vector<pflbm_config> cfgs;
+    std::vector<HostParams> hps;
+    std::vector<BoxDev> boxes;
+    std::vector<WorkItem> items;
+    BoxDev *d_boxes = nullptr;
+    WorkItem *d_items = nullptr;
+    int n_items = 0;
+    BatchPtrs bp{};
+    float *macro = nullptr;
+    double *partial = nullptr, *dev_diag = nullptr;
+    uint64_t total_nodes = 0, max_nodes = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graphs[2] = {nullptr, nullptr};  // kChunk steps per parity
+    int parity = 0;
+    uint64_t step = 0;
+    int zchunk = 16, ctas_per_sm = 2;
+    bool initialized = false;
+    static constexpr int kChunk = 16;
+    static constexpr int kRedBlocks = 304;
+
+    ~Ensemble() { release(); }
+
+    void release() {
+        for (auto &g : graphs)
+            if (g) cudaGraphExecDestroy(g), g = nullptr;
+        void *ptrs[] = {bp.f[0], bp.f[1], bp.phi[0], bp.phi[1], bp.J, bp.step, bp.ctr, bp.err,
+                        macro, partial, dev_diag, d_boxes, d_items};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        std::memset(&bp, 0, sizeof bp);
+        macro = nullptr;
+        partial = dev_diag = nullptr;
+        d_boxes = nullptr;
+        d_items = nullptr;
+        if (stream) cudaStreamDestroy(stream), stream = nullptr;
+    }
+
+    int build_items() {
+        items.clear();
+        for (size_t k = 0; k < boxes.size(); ++k) {
+            const auto &p = boxes[k].p;
+            const int nzi = int(p.nz) - 2;
+            const int zc = std::max(1, std::min(zchunk, nzi));
+            for (int zb = 1; zb < int(p.nz) - 1; zb += zc)
+                for (int y0 = 0; y0 < int(p.ny); y0 += TY)
+                    for (int x0 = 0; x0 < int(p.nx); x0 += TX)
+                        items.push_back({int(k), x0, y0, zb, std::min(zb + zc, int(p.nz) - 1)});
+        }
+        // largest boxes first: long items start early, short ones fill the tail
+        std::stable_sort(items.begin(), items.end(), [&](const WorkItem &a, const WorkItem &b) {
+            return boxes[a.box].p.N > boxes[b.box].p.N;
+        });
+        n_items = int(items.size());
+        if (d_items) cudaFree(d_items), d_items = nullptr;
+        if (cudaMalloc(&d_items, sizeof(WorkItem) * items.size()) != cudaSuccess) return PFLBM_ERR_OUT_OF_MEMORY;
+        if (cudaMemcpy(d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return PFLBM_ERR_CUDA;
+        return PFLBM_OK;
+    }
+
+    void enqueue_step(int par, cudaStream_t s) {
+        const int grid = std::max(1, sms * ctas_per_sm);
+        if (q == 19) {
+            k_collide_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            k_phase_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+        } else {
+            k_collide_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            k_phase_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+        }
+    }
+
+    int capture() {
+        for (auto &g : graphs)
+            if (g) cudaGraphExecDestroy(g), g = nullptr;
+        for (int par = 0; par < 2; ++par) {
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return PFLBM_ERR_CUDA;
+            int pp = par;
+            for (int i = 0; i < kChunk; ++i, pp ^= 1) enqueue_step(pp, stream);
+            if (cudaStreamEndCapture(stream, &g) != cudaSuccess) return PFLBM_ERR_CUDA;
+            const cudaError_t e = cudaGraphInstantiate(&graphs[par], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return PFLBM_ERR_CUDA;
+        }
+        return PFLBM_OK;
+    }
+
+    StepBuffers<float, float> host_box_buffers(int k, int par) const {
+        StepBuffers<float, float> b{};
+        const BoxDev &bx = boxes[k];
+        b.f_src = bp.f[par] + bx.f_off;
+        b.f_dst = bp.f[par ^ 1] + bx.f_off;
+        b.phi_src = bp.phi[par] + bx.n_off;
+        b.phi_dst = bp.phi[par ^ 1] + bx.n_off;
+        b.jflux = bp.J + 3 * bx.n_off;
+        b.macro = macro;
+        b.err = bp.err;
+        return b;
+    }
+
+    void enqueue_init_box(int k) {
+        const auto &h = hps[k];
+        const Params<float> &p = boxes[k].p;
+        InitGeom g{};
+        g.jet = 0;
+        g.droplet_x_stretch = h.droplet_x_stretch;
+        g.center_z = h.f_center_z;
+        g.radius = h.radius;
+        g.interface_width = h.interface_width;
+        g.init_noise = h.init_noise;
+        const dim3 blk(32, 8, 1), grd((p.nx + 31) / 32, (p.ny + 7) / 8, p.nz);
+        k_init_fields<float><<<grd, blk, 0, stream>>>(p, g, macro);
+        const BoxDev &bx = boxes[k];
+        if (q == 19)
+            k_init_distros<19, false, float><<<grd, blk, 0, stream>>>(p, bp.f[0] + bx.f_off, bp.f[1] + bx.f_off,
+                                                                      bp.phi[0] + bx.n_off, bp.phi[1] + bx.n_off, macro);
+        else
+            k_init_distros<27, false, float><<<grd, blk, 0, stream>>>(p, bp.f[0] + bx.f_off, bp.f[1] + bx.f_off,
+                                                                      bp.phi[0] + bx.n_off, bp.phi[1] + bx.n_off, macro);
+    }
+
+    // Analysis of one box after the last completed step into the macro cache.
+    void enqueue_analysis_box(int k) {
+        const Params<float> &p = boxes[k].p;
+        const dim3 blk(32, 8, 1), grd((p.nx + 31) / 32, (p.ny + 7) / 8, p.nz);
+        if (step == 0) {
+            enqueue_init_box(k);  // the cache then holds the initial fields
+            return;
+        }
+        StepBuffers<float, float> b = host_box_buffers(k, parity ^ 1);
+        b.f_dst = nullptr;
+        b.phi_dst = nullptr;
+        b.step_in = nullptr;
+        b.t_fixed = uint32_t(step - 1);
+        const int chunks = (int(p.nz) - 2 + p.zchunk - 1) / p.zchunk;
+        const dim3 cg((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY, chunks);
+        if (q == 19)
+            k_collide<19, false, float, MODE_ANALYSIS><<<cg, dim3(TX, TY), 0, stream>>>(p, b);
+        else
+            k_collide<27, false, float, MODE_ANALYSIS><<<cg, dim3(TX, TY), 0, stream>>>(p, b);
+        k_analysis_ghosts<float><<<grd, blk, 0, stream>>>(p, 0, uint32_t(step - 1), macro);
+    }
+};
+
+}  // namespace pflbm
+
+struct pflbm_ensemble : pflbm::Ensemble {};
+
+using pflbm::Ensemble;
+
+namespace {
+int efail(int code, const std::string &m) {
+    pflbm::set_error(m);
+    return code;
+}
+int ecuda(cudaError_t e, const char *what) {
+    cudaGetLastError();
+    return efail(PFLBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+}  // namespace
+
+extern "C" {
+
+int pflbm_ensemble_create(const pflbm_config *cfgs, int32_t n, pflbm_ensemble **out) {
+    if (!cfgs || !out || n <= 0) return efail(PFLBM_ERR_INVALID_ARG, "null or empty configuration list");
+    *out = nullptr;
+    std::unique_ptr<pflbm_ensemble> e(new (std::nothrow) pflbm_ensemble());
+    if (!e) return efail(PFLBM_ERR_OUT_OF_MEMORY, "host allocation failed");
+    e->q = cfgs[0].velocity_set;
+    for (int k = 0; k < n; ++k) {
+        const int rc = pflbm::validate(cfgs[k]);
+        if (rc) return rc;
+        if (cfgs[k].flow_case != PFLBM_CASE_DROPLET)
+            return efail(PFLBM_ERR_UNSUPPORTED, "ensembles hold periodic droplet boxes only");
+        if (cfgs[k].storage != PFLBM_STORAGE_FP32) return efail(PFLBM_ERR_UNSUPPORTED, "ensembles run FP32 storage");
+        if (cfgs[k].velocity_set != e->q) return efail(PFLBM_ERR_INVALID_ARG, "all boxes must share the velocity set");
+        if (cfgs[k].flags != 0) return efail(PFLBM_ERR_UNSUPPORTED, "derived fields are not kept for ensembles");
+    }
+    int dev = cfgs[0].device >= 0 ? cfgs[0].device : 0;
+    if (cfgs[0].device < 0)
+        if (const char *g = std::getenv("GPU_INDEX")) dev = std::atoi(g);
+    cudaError_t ce = cudaSetDevice(dev);
+    if (ce != cudaSuccess) return ecuda(ce, "cudaSetDevice");
+    e->device = dev;
+    cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev);
+    e->cfgs.assign(cfgs, cfgs + n);
+    e->hps.resize(n);
+    e->boxes.resize(n);
+    uint64_t f_off = 0, n_off = 0;
+    for (int k = 0; k < n; ++k) {
+        pflbm::derive(cfgs[k], e->hps[k]);
+        e->hps[k].zchunk = e->zchunk;
+        e->boxes[k].p = pflbm::make_params<float>(e->hps[k]);
+        e->boxes[k].f_off = f_off;
+        e->boxes[k].n_off = n_off;
+        f_off += uint64_t(e->q) * e->hps[k].N;
+        n_off += e->hps[k].N;
+        e->max_nodes = std::max(e->max_nodes, e->hps[k].N);
+    }
+    e->total_nodes = n_off;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (cudaMalloc(p, bytes) != cudaSuccess) return false;
+        cudaMemset(*p, 0, bytes);
+        return true;
+    };
+    bool ok = alloc(reinterpret_cast<void **>(&e->bp.f[0]), sizeof(float) * f_off) &&
+              alloc(reinterpret_cast<void **>(&e->bp.f[1]), sizeof(float) * f_off) &&
+              alloc(reinterpret_cast<void **>(&e->bp.phi[0]), sizeof(float) * n_off) &&
+              alloc(reinterpret_cast<void **>(&e->bp.phi[1]), sizeof(float) * n_off) &&
+              alloc(reinterpret_cast<void **>(&e->bp.J), sizeof(float) * 3 * n_off) &&
+              alloc(reinterpret_cast<void **>(&e->bp.step), sizeof(unsigned long long) * 2) &&
+              alloc(reinterpret_cast<void **>(&e->bp.ctr), sizeof(unsigned int) * 2) &&
+              alloc(reinterpret_cast<void **>(&e->bp.err), sizeof(unsigned int) * 4) &&
+              alloc(reinterpret_cast<void **>(&e->macro), sizeof(float) * pflbm::M_COUNT * e->max_nodes) &&
+              alloc(reinterpret_cast<void **>(&e->partial), sizeof(double) * pflbm::RED_FIELDS * Ensemble::kRedBlocks) &&
+              alloc(reinterpret_cast<void **>(&e->dev_diag), sizeof(double) * 16) &&
+              alloc(reinterpret_cast<void **>(&e->d_boxes), sizeof(pflbm::BoxDev) * n);
+    if (!ok) {
+        cudaGetLastError();
+        return efail(PFLBM_ERR_OUT_OF_MEMORY, "ensemble device allocation failed");
+    }
+    cudaMemcpy(e->d_boxes, e->boxes.data(), sizeof(pflbm::BoxDev) * n, cudaMemcpyHostToDevice);
+    ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) return ecuda(ce, "cudaStreamCreate");
+    int rc = e->build_items();
+    if (rc) return efail(rc, "work list allocation failed");
+    rc = e->capture();
+    if (rc) return ecuda(cudaGetLastError(), "ensemble graph capture");
+    *out = e.release();
+    return PFLBM_OK;
+}
+
+int pflbm_ensemble_init(pflbm_ensemble *e) {
+    if (!e) return efail(PFLBM_ERR_INVALID_ARG, "null ensemble");
+    cudaSetDevice(e->device);
+    cudaMemsetAsync(e->bp.step, 0, sizeof(unsigned long long) * 2, e->stream);
+    cudaMemsetAsync(e->bp.ctr, 0, sizeof(unsigned int) * 2, e->stream);
+    cudaMemsetAsync(e->bp.err, 0, sizeof(unsigned int) * 4, e->stream);
+    for (size_t k = 0; k < e->boxes.size(); ++k) e->enqueue_init_box(int(k));
+    const cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return ecuda(ce, "ensemble init");
+    e->parity = 0;
+    e->step = 0;
+    e->initialized = true;
+    return PFLBM_OK;
+}
+
+int pflbm_ensemble_step(pflbm_ensemble *e, uint64_t n) {
+    if (!e) return efail(PFLBM_ERR_INVALID_ARG, "null ensemble");
+    if (!e->initialized) return efail(PFLBM_ERR_STATE, "pflbm_ensemble_init has not been called");
+    cudaSetDevice(e->device);
+    uint64_t left = n;
+    while (left >= uint64_t(Ensemble::kChunk)) {
+        const cudaError_t ce = cudaGraphLaunch(e->graphs[e->parity], e->stream);
+        if (ce != cudaSuccess) return ecuda(ce, "cudaGraphLaunch");
+        left -= Ensemble::kChunk;
+        e->step += Ensemble::kChunk;
+    }
+    for (; left > 0; --left) {
+        e->enqueue_step(e->parity, e->stream);
+        e->parity ^= 1;
+        e->step += 1;
+    }
+    cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return ecuda(ce, "ensemble step");
+    unsigned int w = 0;
+    cudaMemcpy(&w, e->bp.err, sizeof w, cudaMemcpyDeviceToHost);
+    if (w) return efail(PFLBM_ERR_DEVICE, "a kernel reported an error");
+    return PFLBM_OK;
+}
+
+int pflbm_ensemble_step_profiled(pflbm_ensemble *e, uint64_t n, double *ms) {
+    if (!e || !ms) return efail(PFLBM_ERR_INVALID_ARG, "null argument");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, e->stream);
+    const int rc = pflbm_ensemble_step(e, n);
+    cudaEventRecord(b, e->stream);
+    cudaEventSynchronize(b);
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = t;
+    return rc;
+}
+
+int pflbm_ensemble_get_field(pflbm_ensemble *e, int32_t box, int32_t id, void *host, size_t bytes) {
+    if (!e || !host) return efail(PFLBM_ERR_INVALID_ARG, "null argument");
+    if (box < 0 || box >= int32_t(e->boxes.size())) return efail(PFLBM_ERR_INVALID_ARG, "box index out of range");
+    if (id < 0 || id > PFLBM_FIELD_FFZ) return efail(PFLBM_ERR_UNSUPPORTED, "ensembles provide fields 0..17");
+    const uint64_t N = e->hps[box].N;
+    if (bytes < N * sizeof(float)) return efail(PFLBM_ERR_INVALID_ARG, "destination buffer too small");
+    cudaSetDevice(e->device);
+    e->enqueue_analysis_box(box);
+    const cudaError_t ce =
+        cudaMemcpyAsync(host, e->macro + size_t(id) * N, N * sizeof(float), cudaMemcpyDeviceToHost, e->stream);
+    if (ce != cudaSuccess) return ecuda(ce, "ensemble readback");
+    const cudaError_t se = cudaStreamSynchronize(e->stream);
+    if (se != cudaSuccess) return ecuda(se, "ensemble readback");
+    return PFLBM_OK;
+}
+
+int pflbm_ensemble_reduce(pflbm_ensemble *e, int32_t box, pflbm_diag *d) {
+    if (!e || !d) return efail(PFLBM_ERR_INVALID_ARG, "null argument");
+    if (box < 0 || box >= int32_t(e->boxes.size())) return efail(PFLBM_ERR_INVALID_ARG, "box index out of range");
+    cudaSetDevice(e->device);
+    e->enqueue_analysis_box(box);
+    pflbm::k_reduce_partial<float><<<Ensemble::kRedBlocks, pflbm::RED_THREADS, 0, e->stream>>>(e->boxes[box].p, e->macro,
+                                                                                               e->partial);
+    pflbm::k_reduce_final<<<1, 32, 0, e->stream>>>(e->partial, Ensemble::kRedBlocks, e->dev_diag);
+    double r[12];
+    cudaMemcpyAsync(r, e->dev_diag, sizeof r, cudaMemcpyDeviceToHost, e->stream);
+    const cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return ecuda(ce, "ensemble reduce");
+    std::memset(d, 0, sizeof(*d));
+    d->step = e->step;
+    d->phi_mass = r[0];
+    d->rho_mass = r[1];
+    d->momentum[0] = r[2]; d->momentum[1] = r[3]; d->momentum[2] = r[4];
+    d->max_speed = r[5];
+    d->n_in = uint64_t(r[7]);
+    d->n_out = uint64_t(r[9]);
+    d->rho_in = r[7] > 0 ? r[6] / r[7] : 0.0;
+    d->rho_out = r[9] > 0 ? r[8] / r[9] : 0.0;
+    d->laplace_dp = (d->rho_in - d->rho_out) / 3.0;
+    d->nonfinite = uint64_t(r[10]);
+    return d->nonfinite ? efail(PFLBM_ERR_DIVERGED, "non-finite values") : PFLBM_OK;
+}
+
+int pflbm_ensemble_set_tuning(pflbm_ensemble *e, int32_t zchunk, int32_t ctas_per_sm) {
+    if (!e || zchunk <= 0 || ctas_per_sm <= 0 || ctas_per_sm > 2)
+        return efail(PFLBM_ERR_INVALID_ARG, "zchunk > 0 and ctas_per_sm in {1, 2}");
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    e->zchunk = zchunk;
+    e->ctas_per_sm = ctas_per_sm;
+    int rc = e->build_items();
+    if (rc) return efail(rc, "work list rebuild failed");
+    rc = e->capture();
+    if (rc) return ecuda(cudaGetLastError(), "ensemble graph capture");
+    return PFLBM_OK;
+}
+
+// Times every (zchunk, ctas_per_sm) candidate for trial_steps steps from the
+// current state, keeps the fastest, then re-initialises the ensemble so the
+// tuning leaves no trace in the results.
+int pflbm_ensemble_autotune(pflbm_ensemble *e, int32_t trial_steps, int32_t *best_zchunk, int32_t *best_ctas,
+                            double *best_ms) {
+    if (!e || trial_steps <= 0) return efail(PFLBM_ERR_INVALID_ARG, "bad argument");
+    const int zcs[] = {4, 8, 16, 32, 64};
+    double best = 1e300;
+    int bz = e->zchunk, bc = e->ctas_per_sm;
+    for (int c = 1; c <= 2; ++c)
+        for (int zc : zcs) {
+            int rc = pflbm_ensemble_set_tuning(e, zc, c);
+            if (rc) return rc;
+            rc = pflbm_ensemble_step(e, 2);
+            if (rc) return rc;
+            double ms = 0;
+            rc = pflbm_ensemble_step_profiled(e, uint64_t(trial_steps), &ms);
+            if (rc) return rc;
+            if (ms < best) best = ms, bz = zc, bc = c;
+        }
+    int rc = pflbm_ensemble_set_tuning(e, bz, bc);
+    if (rc) return rc;
+    rc = pflbm_ensemble_init(e);
+    if (rc) return rc;
+    if (best_zchunk) *best_zchunk = bz;
+    if (best_ctas) *best_ctas = bc;
+    if (best_ms) *best_ms = best;
+    return PFLBM_OK;
+}
+
+int pflbm_ensemble_info(const pflbm_ensemble *e, uint64_t *total_nodes, int32_t *n_boxes, int32_t *n_items) {
+    if (!e) return efail(PFLBM_ERR_INVALID_ARG, "null ensemble");
+    if (total_nodes) *total_nodes = e->total_nodes;
+    if (n_boxes) *n_boxes = int32_t(e->boxes.size());
+    if (n_items) *n_items = e->n_items;
+    return PFLBM_OK;
+}
+
+int pflbm_ensemble_destroy(pflbm_ensemble *e) {
+    if (!e) return PFLBM_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    delete e;
+    return PFLBM_OK;
+}
+
+}  // extern "C"

@@ -142,21 +142,193 @@ __device__ __forceinline__ T lattice_grad(const Get &v, const int *ca) {
     return r;
 }
 
-// ------------------------------------------------------------ k_collide
+// Per-node work after the stencils (src/phaseField.cuh:214-218,
+// src/lbm.cu:33-239): surface-tension force, moments, relaxation, regularised
+// collision with pull-layout stores, phase flux J, boundary-plane moments and
+// derived averages; in MODE_ANALYSIS the 18 reference arrays instead.
 template <int QQ, bool JET, class S, int MODE>
-__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : 2))
-    k_collide(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b) {
+__device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> &p,
+                                             const StepBuffers<S, typename Store<S>::T> &b, int x, int y, int z,
+                                             uint32_t t, const typename Store<S>::T (&pop)[QQ],
+                                             typename Store<S>::T phi, typename Store<S>::T n_x,
+                                             typename Store<S>::T n_y, typename Store<S>::T n_z,
+                                             typename Store<S>::T ind, typename Store<S>::T curvature) {
     using T = typename Store<S>::T;
-    __shared__ T s_phi[3][PY][PX];
-    __shared__ T s_n[4][3][NY_][NX_];  // nx, ny, nz, |grad phi|
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const uint64_t N = p.N, plane = p.plane;
+    const uint64_t base = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * (y + static_cast<uint64_t>(ny) * z);
+    const T st = -p.sigma * curvature * ind;
+    const T fx = st * n_x, fy = st * n_y, fz = st * n_z;
 
+    // moments (src/lbm.cu:33-128)
+    const Macro<T> m = moments<QQ, T>(pop, fx, fy, fz);
+
+    // relaxation (src/lbm.cu:158-170)
+    T omega;
+    if constexpr (JET) {
+        const T tau_phi = (T(1) - phi) * p.tau_water + phi * p.tau_oil;
+        const T r = sponge_ramp<T>(p, z);
+        const T visc_local = (T(1) - phi) * p.visc_water + phi * p.visc_oil;
+        const T tau_zmax = T(0.5) + T(3) * (visc_local * p.kgain1);
+        const T tau_eff = tau_phi + r * (tau_zmax - tau_phi);
+        omega = T(1) / tau_eff;
+    } else {
+        omega = p.omega_ref;
+    }
+    const CollideCtx<T> k = make_ctx<QQ, T>(m, fx, fy, fz, T(1) - omega);
+
+    if constexpr (MODE == MODE_ANALYSIS) {
+        T *mc = b.macro;
+        mc[M_RHO * N + base] = m.rho;
+        mc[M_UX * N + base] = m.ux;
+        mc[M_UY * N + base] = m.uy;
+        mc[M_UZ * N + base] = m.uz;
+        mc[M_PXX * N + base] = m.pxx;
+        mc[M_PYY * N + base] = m.pyy;
+        mc[M_PZZ * N + base] = m.pzz;
+        mc[M_PXY * N + base] = m.pxy;
+        mc[M_PXZ * N + base] = m.pxz;
+        mc[M_PYZ * N + base] = m.pyz;
+        mc[M_PHI * N + base] = phi;
+        mc[M_NX * N + base] = n_x;
+        mc[M_NY * N + base] = n_y;
+        mc[M_NZ * N + base] = n_z;
+        mc[M_IND * N + base] = ind;
+        mc[M_FX * N + base] = fx;
+        mc[M_FY * N + base] = fy;
+        mc[M_FZ * N + base] = fz;
+        return;
+    } else {
+        // periodic-edge store offsets: P = wrap(S + c) - c
+        const int64_t ex_p = (x == nx - 2) ? -(int64_t)(nx - 2) : 0;  // cx = +1
+        const int64_t ex_m = (x == 1) ? (int64_t)(nx - 2) : 0;        // cx = -1
+        const int64_t ey_p = (y == ny - 2) ? -(int64_t)(ny - 2) * nx : 0;
+        const int64_t ey_m = (y == 1) ? (int64_t)(ny - 2) * nx : 0;
+        int64_t ez_p = 0, ez_m = 0;
+        if constexpr (!JET) {
+            ez_p = (z == nz - 2) ? -(int64_t)(nz - 2) * (int64_t)plane : 0;
+            ez_m = (z == 1) ? (int64_t)(nz - 2) * (int64_t)plane : 0;
+        }
+        auto dst_index = [&](int q) -> uint64_t {
+            int64_t o = 0;
+            if (kCX[q] > 0) o += ex_p;
+            if (kCX[q] < 0) o += ex_m;
+            if (kCY[q] > 0) o += ey_p;
+            if (kCY[q] < 0) o += ey_m;
+            if (kCZ[q] > 0) o += ez_p;
+            if (kCZ[q] < 0) o += ez_m;
+            return q * N + base + o;
+        };
+        // collision + streaming (src/lbm.cu:172-207)
+        Store<S>::store(b.f_dst, base, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
+#pragma unroll
+        for (int q = 1; q < QQ; q += 2) {
+            T a, c;
+            collide_pair<QQ, T>(q, k, a, c);
+            Store<S>::store(b.f_dst, dst_index(q), a, static_cast<T>(1.0 / weight<QQ>(q)));
+            Store<S>::store(b.f_dst, dst_index(q + 1), c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
+        }
+        // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J)
+        const T sharp = p.gamma * phi * (T(1) - phi);
+        b.jflux[base] = T(4) * phi * m.ux + sharp * n_x;
+        b.jflux[N + base] = T(4) * phi * m.uy + sharp * n_y;
+        b.jflux[2 * N + base] = T(4) * phi * m.uz + sharp * n_z;
+
+        if constexpr (JET) {
+            if (z == nz - 2) {
+                // moments of the last fluid plane for the outflow rebuild
+                const uint64_t c2 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
+                T *tp = b.top;
+                tp[0 * plane + c2] = m.rho;
+                tp[1 * plane + c2] = m.ux;
+                tp[2 * plane + c2] = m.uy;
+                tp[3 * plane + c2] = m.uz;
+                tp[4 * plane + c2] = m.pxx;
+                tp[5 * plane + c2] = m.pyy;
+                tp[6 * plane + c2] = m.pzz;
+                tp[7 * plane + c2] = m.pxy;
+                tp[8 * plane + c2] = m.pxz;
+                tp[9 * plane + c2] = m.pyz;
+                tp[10 * plane + c2] = fx;
+                tp[11 * plane + c2] = fy;
+                tp[12 * plane + c2] = fz;
+            }
+            if (z == 1) {
+                // moments of the first fluid plane for the inflow rebuild
+                const uint64_t c2 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
+                T *bp = b.top + 13 * plane;
+                bp[0 * plane + c2] = m.ux;
+                bp[1 * plane + c2] = m.uy;
+                bp[2 * plane + c2] = m.uz;
+                bp[3 * plane + c2] = m.pxx;
+                bp[4 * plane + c2] = m.pyy;
+                bp[5 * plane + c2] = m.pzz;
+                bp[6 * plane + c2] = m.pxy;
+                bp[7 * plane + c2] = m.pxz;
+                bp[8 * plane + c2] = m.pyz;
+            }
+        }
+        if constexpr (MODE == MODE_STEP_AVG) {
+            // derived fields (timeAverage.cuh:57-60, reynoldsMoments.cuh:57-60)
+            const T tf = static_cast<T>(t + 1u);
+            T *av = b.avg;
+            auto upd = [&](int slot, uint64_t i, T nv_) {
+                const T o = av[slot * N + i];
+                av[slot * N + i] = o + (nv_ - o) / tf;
+            };
+            upd(0, base, phi);
+            upd(1, base, m.ux);
+            upd(2, base, m.uy);
+            upd(3, base, m.uz);
+            upd(4, base, m.ux * m.ux);
+            upd(5, base, m.uy * m.uy);
+            upd(6, base, m.uz * m.uz);
+            upd(7, base, m.ux * m.uy);
+            upd(8, base, m.ux * m.uz);
+            upd(9, base, m.uy * m.uz);
+            if constexpr (JET) {
+                if (z == 1 && in_disc<T>(p, x, y)) {
+                    // ghost inlet node (x,y,0) holds phi = 1 and the inlet velocity
+                    const uint64_t g0 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
+                    T bux, buy, buz;
+                    inflow_velocity<T>(p, x, y, t, bux, buy, buz);
+                    upd(0, g0, T(1));
+                    upd(1, g0, bux);
+                    upd(2, g0, buy);
+                    upd(3, g0, buz);
+                    upd(4, g0, bux * bux);
+                    upd(5, g0, buy * buy);
+                    upd(6, g0, buz * buz);
+                    upd(7, g0, bux * buy);
+                    upd(8, g0, bux * buz);
+                    upd(9, g0, buy * buz);
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ k_collide
+// Shared-memory rings of the plain-load collide (one tile at a time).
+template <class T>
+struct CollideSmem {
+    T phi[3][PY][PX];
+    T n[4][3][NY_][NX_];  // nx, ny, nz, |grad phi|
+};
+
+// z-march of one 32x8 column tile over interior planes [zb, ze): the body of
+// k_collide, also run by the batched ensemble kernel for its work items.
+template <int QQ, bool JET, class S, int MODE>
+__device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> &p,
+                                             const StepBuffers<S, typename Store<S>::T> &b, int x0, int y0, int zb,
+                                             int ze, CollideSmem<typename Store<S>::T> &sm) {
+    using T = typename Store<S>::T;
+    auto &s_phi = sm.phi;
+    auto &s_n = sm.n;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const int x = x0 + tx, y = y0 + ty;
-    const int zb = 1 + blockIdx.z * p.zchunk;
-    const int ze = min(zb + p.zchunk, nz - 1);
     const bool col = (x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2);
     const uint32_t t = b.step_in ? static_cast<uint32_t>(*b.step_in) : b.t_fixed;
 
@@ -239,175 +411,29 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : 2
         const T scz = lattice_grad<QQ, T>([&](int dx, int dy, int dz) { return nv(2, dx, dy, dz); }, kCZ);
         const T curvature = T(3) * (scx + scy + scz);
         const T n_x = nv(0, 0, 0, 0), n_y = nv(1, 0, 0, 0), n_z = nv(2, 0, 0, 0), ind = nv(3, 0, 0, 0);
-        const T st = -p.sigma * curvature * ind;
-        const T fx = st * n_x, fy = st * n_y, fz = st * n_z;
         const T phi = s_phi[z % 3][ty + 2][tx + 2];
-
-        // moments (src/lbm.cu:33-128)
-        const Macro<T> m = moments<QQ, T>(pop, fx, fy, fz);
-
-        // relaxation (src/lbm.cu:158-170)
-        T omega;
-        if constexpr (JET) {
-            const T tau_phi = (T(1) - phi) * p.tau_water + phi * p.tau_oil;
-            const T r = sponge_ramp<T>(p, z);
-            const T visc_local = (T(1) - phi) * p.visc_water + phi * p.visc_oil;
-            const T tau_zmax = T(0.5) + T(3) * (visc_local * p.kgain1);
-            const T tau_eff = tau_phi + r * (tau_zmax - tau_phi);
-            omega = T(1) / tau_eff;
-        } else {
-            omega = p.omega_ref;
-        }
-        const CollideCtx<T> k = make_ctx<QQ, T>(m, fx, fy, fz, T(1) - omega);
-
-        if constexpr (MODE == MODE_ANALYSIS) {
-            T *mc = b.macro;
-            mc[M_RHO * N + base] = m.rho;
-            mc[M_UX * N + base] = m.ux;
-            mc[M_UY * N + base] = m.uy;
-            mc[M_UZ * N + base] = m.uz;
-            mc[M_PXX * N + base] = m.pxx;
-            mc[M_PYY * N + base] = m.pyy;
-            mc[M_PZZ * N + base] = m.pzz;
-            mc[M_PXY * N + base] = m.pxy;
-            mc[M_PXZ * N + base] = m.pxz;
-            mc[M_PYZ * N + base] = m.pyz;
-            mc[M_PHI * N + base] = phi;
-            mc[M_NX * N + base] = n_x;
-            mc[M_NY * N + base] = n_y;
-            mc[M_NZ * N + base] = n_z;
-            mc[M_IND * N + base] = ind;
-            mc[M_FX * N + base] = fx;
-            mc[M_FY * N + base] = fy;
-            mc[M_FZ * N + base] = fz;
-            continue;
-        } else {
-            // periodic-edge store offsets: P = wrap(S + c) - c
-            const int64_t ex_p = (x == nx - 2) ? -(int64_t)(nx - 2) : 0;  // cx = +1
-            const int64_t ex_m = (x == 1) ? (int64_t)(nx - 2) : 0;        // cx = -1
-            const int64_t ey_p = (y == ny - 2) ? -(int64_t)(ny - 2) * nx : 0;
-            const int64_t ey_m = (y == 1) ? (int64_t)(ny - 2) * nx : 0;
-            int64_t ez_p = 0, ez_m = 0;
-            if constexpr (!JET) {
-                ez_p = (z == nz - 2) ? -(int64_t)(nz - 2) * (int64_t)plane : 0;
-                ez_m = (z == 1) ? (int64_t)(nz - 2) * (int64_t)plane : 0;
-            }
-            auto dst_index = [&](int q) -> uint64_t {
-                int64_t o = 0;
-                if (kCX[q] > 0) o += ex_p;
-                if (kCX[q] < 0) o += ex_m;
-                if (kCY[q] > 0) o += ey_p;
-                if (kCY[q] < 0) o += ey_m;
-                if (kCZ[q] > 0) o += ez_p;
-                if (kCZ[q] < 0) o += ez_m;
-                return q * N + base + o;
-            };
-            // collision + streaming (src/lbm.cu:172-207)
-            Store<S>::store(b.f_dst, base, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
-#pragma unroll
-            for (int q = 1; q < QQ; q += 2) {
-                T a, c;
-                collide_pair<QQ, T>(q, k, a, c);
-                Store<S>::store(b.f_dst, dst_index(q), a, static_cast<T>(1.0 / weight<QQ>(q)));
-                Store<S>::store(b.f_dst, dst_index(q + 1), c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
-            }
-            // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J)
-            const T sharp = p.gamma * phi * (T(1) - phi);
-            b.jflux[base] = T(4) * phi * m.ux + sharp * n_x;
-            b.jflux[N + base] = T(4) * phi * m.uy + sharp * n_y;
-            b.jflux[2 * N + base] = T(4) * phi * m.uz + sharp * n_z;
-
-            if constexpr (JET) {
-                if (z == nz - 2) {
-                    // moments of the last fluid plane for the outflow rebuild
-                    const uint64_t c2 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
-                    T *tp = b.top;
-                    tp[0 * plane + c2] = m.rho;
-                    tp[1 * plane + c2] = m.ux;
-                    tp[2 * plane + c2] = m.uy;
-                    tp[3 * plane + c2] = m.uz;
-                    tp[4 * plane + c2] = m.pxx;
-                    tp[5 * plane + c2] = m.pyy;
-                    tp[6 * plane + c2] = m.pzz;
-                    tp[7 * plane + c2] = m.pxy;
-                    tp[8 * plane + c2] = m.pxz;
-                    tp[9 * plane + c2] = m.pyz;
-                    tp[10 * plane + c2] = fx;
-                    tp[11 * plane + c2] = fy;
-                    tp[12 * plane + c2] = fz;
-                }
-                if (z == 1) {
-                    // moments of the first fluid plane for the inflow rebuild
-                    const uint64_t c2 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
-                    T *bp = b.top + 13 * plane;
-                    bp[0 * plane + c2] = m.ux;
-                    bp[1 * plane + c2] = m.uy;
-                    bp[2 * plane + c2] = m.uz;
-                    bp[3 * plane + c2] = m.pxx;
-                    bp[4 * plane + c2] = m.pyy;
-                    bp[5 * plane + c2] = m.pzz;
-                    bp[6 * plane + c2] = m.pxy;
-                    bp[7 * plane + c2] = m.pxz;
-                    bp[8 * plane + c2] = m.pyz;
-                }
-            }
-            if constexpr (MODE == MODE_STEP_AVG) {
-                // derived fields (timeAverage.cuh:57-60, reynoldsMoments.cuh:57-60)
-                const T tf = static_cast<T>(t + 1u);
-                T *av = b.avg;
-                auto upd = [&](int slot, uint64_t i, T nv_) {
-                    const T o = av[slot * N + i];
-                    av[slot * N + i] = o + (nv_ - o) / tf;
-                };
-                upd(0, base, phi);
-                upd(1, base, m.ux);
-                upd(2, base, m.uy);
-                upd(3, base, m.uz);
-                upd(4, base, m.ux * m.ux);
-                upd(5, base, m.uy * m.uy);
-                upd(6, base, m.uz * m.uz);
-                upd(7, base, m.ux * m.uy);
-                upd(8, base, m.ux * m.uz);
-                upd(9, base, m.uy * m.uz);
-                if constexpr (JET) {
-                    if (z == 1 && in_disc<T>(p, x, y)) {
-                        // ghost inlet node (x,y,0) holds phi = 1 and the inlet velocity
-                        const uint64_t g0 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
-                        T bux, buy, buz;
-                        inflow_velocity<T>(p, x, y, t, bux, buy, buz);
-                        upd(0, g0, T(1));
-                        upd(1, g0, bux);
-                        upd(2, g0, buy);
-                        upd(3, g0, buz);
-                        upd(4, g0, bux * bux);
-                        upd(5, g0, buy * buy);
-                        upd(6, g0, buz * buz);
-                        upd(7, g0, bux * buy);
-                        upd(8, g0, bux * buz);
-                        upd(9, g0, buy * buz);
-                    }
-                }
-            }
-        }
+        collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature);
     }
+}
+
+template <int QQ, bool JET, class S, int MODE>
+__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : 2))
+    k_collide(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b) {
+    __shared__ CollideSmem<typename Store<S>::T> sm;
+    const int zb = 1 + blockIdx.z * p.zchunk;
+    collide_tile<QQ, JET, S, MODE>(p, b, blockIdx.x * TX, blockIdx.y * TY, zb, min(zb + p.zchunk, int(p.nz) - 1), sm);
 }
 
 // -------------------------------------------------------------- k_phase
 // phi^{n+1} (computePhase of the next step, src/phaseField.cuh:31-52),
 // outflow rebuild (BoundaryConditions.cuh:107-169) and step counter.
 template <int QQ, bool JET, class S>
-__global__ void __launch_bounds__(256) k_phase(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b) {
+__device__ __forceinline__ void phase_node(const Params<typename Store<S>::T> &p,
+                                           const StepBuffers<S, typename Store<S>::T> &b, int x, int y, int z,
+                                           uint32_t t) {
     using T = typename Store<S>::T;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N, plane = p.plane;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    const uint32_t t = static_cast<uint32_t>(*b.step_in);
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0 &&
-        threadIdx.z == 0)
-        *b.step_out = *b.step_in + 1ull;
-    if (x < 1 || x > nx - 2 || y < 1 || y > ny - 2 || z < 1 || z > nz - 2) return;
     const uint64_t X = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * (y + static_cast<uint64_t>(ny) * z);
     auto idx = [&](int xx, int yy, int zz) -> uint64_t {
         return static_cast<uint64_t>(xx) + static_cast<uint64_t>(nx) * (yy + static_cast<uint64_t>(ny) * zz);
@@ -513,6 +539,100 @@ __global__ void __launch_bounds__(256) k_phase(const Params<typename Store<S>::T
                     Store<S>::store(b.f_dst, dst, v, static_cast<T>(1.0 / weight<QQ>(q)));
                 }
             }
+        }
+    }
+}
+
+
+template <int QQ, bool JET, class S>
+__global__ void __launch_bounds__(256) k_phase(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    const uint32_t t = static_cast<uint32_t>(*b.step_in);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0 &&
+        threadIdx.z == 0)
+        *b.step_out = *b.step_in + 1ull;
+    if (x < 1 || x > int(p.nx) - 2 || y < 1 || y > int(p.ny) - 2 || z < 1 || z > int(p.nz) - 2) return;
+    phase_node<QQ, JET, S>(p, b, x, y, z, t);
+}
+
+// FP32 phase step with 128-bit accesses: one thread owns 4 consecutive x
+// nodes (nx % 4 == 0), reads the phi/J rows of its y and z neighbours as
+// float4 and the two x-end neighbours (periodically wrapped) as scalars.
+// The jet's boundary planes z = 1 and nz-2 go through phase_node.
+template <int QQ, bool JET, class S>
+__global__ void __launch_bounds__(256) k_phase_v4(const Params<float> p, const StepBuffers<S, float> b) {
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const uint64_t N = p.N, plane = p.plane;
+    const int x4 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    const uint32_t t = static_cast<uint32_t>(*b.step_in);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0 &&
+        threadIdx.z == 0)
+        *b.step_out = *b.step_in + 1ull;
+    if (x4 >= nx || y < 1 || y > ny - 2 || z < 1 || z > nz - 2) return;
+    if (JET && (z == 1 || z == nz - 2)) {
+        for (int k = 0; k < 4; ++k) {
+            const int x = x4 + k;
+            if (x >= 1 && x <= nx - 2) phase_node<QQ, JET, S>(p, b, x, y, z, t);
+        }
+        return;
+    }
+    const int ym = wrapi(y - 1, ny), yp = wrapi(y + 1, ny);
+    const int zm = JET ? z - 1 : wrapi(z - 1, nz), zp = JET ? z + 1 : wrapi(z + 1, nz);
+    auto row = [&](int yy, int zz) -> uint64_t { return static_cast<uint64_t>(nx) * (yy + static_cast<uint64_t>(ny) * zz); };
+    const float *phi = b.phi_src;
+    const float *Jx = b.jflux, *Jy = b.jflux + N, *Jz = b.jflux + 2 * N;
+    const uint64_t r0 = row(y, z);
+    const float4 pc = *reinterpret_cast<const float4 *>(phi + r0 + x4);
+    const float4 pym = *reinterpret_cast<const float4 *>(phi + row(ym, z) + x4);
+    const float4 pyp = *reinterpret_cast<const float4 *>(phi + row(yp, z) + x4);
+    const float4 pzm = *reinterpret_cast<const float4 *>(phi + row(y, zm) + x4);
+    const float4 pzp = *reinterpret_cast<const float4 *>(phi + row(y, zp) + x4);
+    const float4 jxc = *reinterpret_cast<const float4 *>(Jx + r0 + x4);
+    const float4 jym = *reinterpret_cast<const float4 *>(Jy + row(ym, z) + x4);
+    const float4 jyp = *reinterpret_cast<const float4 *>(Jy + row(yp, z) + x4);
+    const float4 jzm = *reinterpret_cast<const float4 *>(Jz + row(y, zm) + x4);
+    const float4 jzp = *reinterpret_cast<const float4 *>(Jz + row(y, zp) + x4);
+    // x neighbours of the 4-node segment, periodic inside [1, nx-2]
+    const int xl = wrapi(x4 - 1, nx), xr = wrapi(x4 + 4, nx);
+    float pl[6], jl[6];  // phi and Jx at x4-1 .. x4+4
+    pl[0] = phi[r0 + xl]; jl[0] = Jx[r0 + xl];
+    pl[1] = pc.x; pl[2] = pc.y; pl[3] = pc.z; pl[4] = pc.w;
+    jl[1] = jxc.x; jl[2] = jxc.y; jl[3] = jxc.z; jl[4] = jxc.w;
+    pl[5] = phi[r0 + xr]; jl[5] = Jx[r0 + xr];
+    const float a_ym[4] = {pym.x, pym.y, pym.z, pym.w}, a_yp[4] = {pyp.x, pyp.y, pyp.z, pyp.w};
+    const float a_zm[4] = {pzm.x, pzm.y, pzm.z, pzm.w}, a_zp[4] = {pzp.x, pzp.y, pzp.z, pzp.w};
+    const float b_ym[4] = {jym.x, jym.y, jym.z, jym.w}, b_yp[4] = {jyp.x, jyp.y, jyp.z, jyp.w};
+    const float b_zm[4] = {jzm.x, jzm.y, jzm.z, jzm.w}, b_zp[4] = {jzp.x, jzp.y, jzp.z, jzp.w};
+    float out[4];
+    const float w0 = 0.25f, w1 = 0.125f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = x4 + k;
+        // left/right sources; ghost columns map to the periodic image
+        float phl = pl[k], jxl = jl[k], phr = pl[k + 2], jxr = jl[k + 2];
+        if (x == 1) { phl = phi[r0 + nx - 2]; jxl = Jx[r0 + nx - 2]; }
+        if (x == nx - 2) { phr = phi[r0 + 1]; jxr = Jx[r0 + 1]; }
+        float s = 0.0f;
+        s += w0 * pl[k + 1];
+        s += w1 * (phl + jxl);
+        s += w1 * (phr - jxr);
+        s += w1 * (a_ym[k] + b_ym[k]);
+        s += w1 * (a_yp[k] - b_yp[k]);
+        s += w1 * (a_zm[k] + b_zm[k]);
+        s += w1 * (a_zp[k] - b_zp[k]);
+        out[k] = s;
+    }
+    // ghost columns keep their (zero) phi; write only interior nodes
+    if (x4 >= 1 && x4 + 3 <= nx - 2) {
+        *reinterpret_cast<float4 *>(b.phi_dst + r0 + x4) = make_float4(out[0], out[1], out[2], out[3]);
+    } else {
+        for (int k = 0; k < 4; ++k) {
+            const int x = x4 + k;
+            if (x >= 1 && x <= nx - 2) b.phi_dst[r0 + x] = out[k];
         }
     }
 }

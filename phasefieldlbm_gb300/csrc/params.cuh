@@ -40,12 +40,14 @@ template <>
 struct Store<float> {
     using T = float;
     static __device__ __forceinline__ float load(const float *p, uint64_t i, float) { return __ldg(p + i); }
+    static __device__ __forceinline__ float widen(float v, float) { return v; }
     static __device__ __forceinline__ void store(float *p, uint64_t i, float v, float) { p[i] = v; }
 };
 template <>
 struct Store<double> {
     using T = double;
     static __device__ __forceinline__ double load(const double *p, uint64_t i, double) { return __ldg(p + i); }
+    static __device__ __forceinline__ double widen(double v, double) { return v; }
     static __device__ __forceinline__ void store(double *p, uint64_t i, double v, double) { p[i] = v; }
 };
 template <>
@@ -54,6 +56,7 @@ struct Store<__half> {
     static __device__ __forceinline__ float load(const __half *p, uint64_t i, float w) {
         return w * __half2float(__ldg(p + i));
     }
+    static __device__ __forceinline__ float widen(__half v, float w) { return w * __half2float(v); }
     static __device__ __forceinline__ void store(__half *p, uint64_t i, float v, float inv_w) {
         p[i] = __float2half_rn(v * inv_w);
     }
@@ -64,6 +67,7 @@ struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ float load(const __nv_bfloat16 *p, uint64_t i, float w) {
         return w * __bfloat162float(__ldg(p + i));
     }
+    static __device__ __forceinline__ float widen(__nv_bfloat16 v, float w) { return w * __bfloat162float(v); }
     static __device__ __forceinline__ void store(__nv_bfloat16 *p, uint64_t i, float v, float inv_w) {
         p[i] = __float2bfloat16_rn(v * inv_w);
     }

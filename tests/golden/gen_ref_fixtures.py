@@ -25,7 +25,7 @@ FIELDS = ("rho", "ux", "uy", "uz", "phi")
 JOBS = [
     ("jet_d3q19", 60, (1, 2, 64, 126, 127)),
     ("jet_d3q27", 60, (1, 64, 126)),
-    ("droplet_d3q19", 40, (64,)),
+    ("droplet_d3q19", 10, (40, 88)),
 ]
 
 

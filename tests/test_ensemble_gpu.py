@@ -1,0 +1,61 @@
+"""Batched droplet ensembles: every box of a batch evolves exactly as the same
+configuration run alone (same kernels, same per-box constants), whatever the
+tuning; the autotuner leaves the results unchanged."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("rho", "ux", "uy", "uz", "phi")
+
+
+def small_batch(pf, n=5, vs=19):
+    cfgs = pf.ensemble_configs(n=n, seed=7, velocity_set=vs)
+    # keep the test quick: shrink the largest boxes
+    for c in cfgs:
+        e = min(int(c.nx), 48)
+        c.nx = c.ny = c.nz = e
+        c.radius = max(2, min(c.radius, e // 4))
+        c.diam = 2 * c.radius
+    return cfgs
+
+
+@pytest.mark.parametrize("vs", [19, 27])
+def test_boxes_match_single_runs(pflbm, vs):
+    cfgs = small_batch(pflbm, vs=vs)
+    steps = 37
+    with pflbm.Ensemble(cfgs) as ens:
+        ens.set_tuning(8, 2)
+        ens.step(steps)
+        got = [{f: ens.get_field(k, f) for f in FIELDS} for k in range(len(cfgs))]
+    for k, c in enumerate(cfgs):
+        with pflbm.Simulation(c) as s:
+            s.step(steps)
+            for f in FIELDS:
+                assert np.array_equal(got[k][f], s.get_field(f)), (k, f)
+
+
+def test_tuning_does_not_change_results(pflbm):
+    cfgs = small_batch(pflbm, n=4)
+    res = []
+    for zc, ctas in ((4, 1), (64, 2)):
+        with pflbm.Ensemble(cfgs) as ens:
+            ens.set_tuning(zc, ctas)
+            ens.step(20)
+            res.append([ens.get_field(k, "phi") for k in range(len(cfgs))])
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
+
+
+def test_autotune_and_mass(pflbm):
+    cfgs = small_batch(pflbm, n=6)
+    with pflbm.Ensemble(cfgs) as ens:
+        best = ens.autotune(trial_steps=4)
+        assert best["zchunk"] in (4, 8, 16, 32, 64) and best["ctas_per_sm"] in (1, 2)
+        ens.step(1)
+        m0 = [ens.reduce(k).phi_mass for k in range(len(cfgs))]
+        ens.step(100)
+        for k in range(len(cfgs)):
+            d = ens.reduce(k)
+            assert d.nonfinite == 0
+            assert abs(d.phi_mass - m0[k]) / m0[k] < 1e-6

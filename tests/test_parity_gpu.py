@@ -8,12 +8,13 @@ fused two-kernel pull step. Tolerances:
     step order, noise) exactly. The reference's Gaussian inflow noise is
     computed in float with logf/cosf, whose last-ulp results differ between
     the host libm and CUDA; jets in that mode are held to 1e-7 instead.
-  * FP32 vs FP32 oracle: rel. L2 <= 1e-5 on rho, phi and the velocity vector
-    field u (the tolerance of the FP32 plain path). Each velocity component
-    must also lie within 2x the FP32 rounding floor of the case, measured as
-    the oracle's own FP32-vs-FP64 difference (ux, uy of a young jet are pure
-    inflow noise and sit near 1e-5 in any FP32 implementation). Pi and F,
-    small differences of large terms, are held to 1e-3.
+  * FP32 vs FP32 oracle: rel. L2 <= 1e-5 on rho and phi. The velocity of a
+    static droplet or a young jet is small, and its relative L2 floor in any
+    FP32 implementation, measured here as the oracle's own FP32-vs-FP64
+    difference on the same case and horizon, lies between 3e-6 and 5e-5; u
+    (the vector field and each component) must be within
+    max(1e-5, 2 x floor). Pi and F, small differences of large terms, are
+    held to 1e-3.
 """
 import numpy as np
 import pytest
@@ -66,7 +67,10 @@ def run_pair(pf, oracle, cfg, steps, fp64=False, fields=BASIC, floor=False):
     if floor:
         o64 = oracle.OracleSim(c, fp64=True)
         o64.step(steps)
-        errs["floor"] = {f: rel_l2(ora[f], o64.get_field(f)) for f in ("rho", "ux", "uy", "uz", "phi")}
+        fl = {f: rel_l2(ora[f], o64.get_field(f)) for f in ("rho", "ux", "uy", "uz", "phi")}
+        fl["u"] = rel_l2(np.stack([ora[f] for f in ("ux", "uy", "uz")]),
+                         np.stack([o64.get_field(f) for f in ("ux", "uy", "uz")]))
+        errs["floor"] = fl
     return errs
 
 
@@ -93,8 +97,8 @@ def test_fp64_semantics(pflbm, oracle, name, make, steps):
 def test_fp32_parity(pflbm, oracle, name, make, steps):
     errs = run_pair(pflbm, oracle, make(pflbm), steps, fp64=False, fields=ALL18, floor=True)
     floor = errs.pop("floor")
-    bad = {k: errs[k] for k in ("rho", "phi", "u") if not errs[k] <= 1e-5}
-    bad.update({k: errs[k] for k in ("ux", "uy", "uz") if not errs[k] <= max(1e-5, 2.0 * floor[k])})
+    bad = {k: errs[k] for k in ("rho", "phi") if not errs[k] <= 1e-5}
+    bad.update({k: errs[k] for k in ("u", "ux", "uy", "uz") if not errs[k] <= max(1e-5, 2.0 * floor[k])})
     bad.update({k: v for k, v in errs.items() if k not in BASIC + ("u",) and not v <= 1e-3})
     assert not bad, (errs, floor)
 
@@ -196,3 +200,54 @@ def test_write_output_layout(pflbm, tmp_path):
         assert vti.startswith(b'<?xml version="1.0"?>')
         assert b'WholeExtent="0 15 0 15 0 15"' in vti
         assert b'Name="uz" NumberOfComponents="1" format="appended" offset="16388"' in vti
+
+
+@pytest.mark.parametrize("vs,storage", [(19, 0), (27, 0), (19, 1), (27, 2), (19, 3)])
+def test_tma_and_vector_paths_bit_identical(pflbm, monkeypatch, vs, storage):
+    # The TMA-fed collide kernel and the float4 phase kernel compute exactly
+    # what the plain-load kernels compute; only the data movement differs.
+    c = jet_cfg(pflbm, vs, nx=64, ny=40, nz=48, diam=10, noise=1)
+    c.storage = storage
+    out = {}
+    for mode in ("fast", "plain"):
+        if mode == "plain":
+            monkeypatch.setenv("PFLBM_NO_TMA", "1")
+            monkeypatch.setenv("PFLBM_NO_VEC", "1")
+        with pflbm.Simulation(c) as s:
+            if mode == "fast":
+                assert s.uses_tma
+            else:
+                assert not s.uses_tma
+            s.step(33)
+            out[mode] = {f: s.get_field(f, dtype=np.float64) for f in ALL18}
+    for f in ALL18:
+        assert np.array_equal(out["fast"][f], out["plain"][f]), f
+
+
+@pytest.mark.parametrize("storage", [0, 1])
+def test_checkpoint_resume_bit_identical(pflbm, tmp_path, storage):
+    c = jet_cfg(pflbm, 27, nx=32, ny=32, nz=48, diam=8, noise=1)
+    c.storage = storage
+    c.flags = pflbm.FLAG_TIME_AVERAGE
+    ck = tmp_path / "state.ckpt"
+    with pflbm.Simulation(c) as a:
+        a.step(31)
+        a.save_checkpoint(ck)
+        a.step(20)
+        want = {f: a.get_field(f) for f in BASIC + ("avg_uz",)}
+    with pflbm.Simulation(c) as a2:
+        a2.step(31)
+        at31 = {f: a2.get_field(f) for f in ALL18}
+    with pflbm.Simulation(c, init=False) as b:
+        b.load_checkpoint(ck)
+        assert b.current_step == 31
+        for f in ALL18:  # readback right after a load is the step-31 state
+            assert np.array_equal(b.get_field(f), at31[f]), f
+        b.step(20)
+        for f, v in want.items():
+            assert np.array_equal(b.get_field(f), v), f
+    bad = c.copy()
+    bad.nz = 50
+    with pflbm.Simulation(bad, init=False) as d:
+        with pytest.raises(pflbm.PflbmError):
+            d.load_checkpoint(ck)
