@@ -215,6 +215,79 @@ Consts<T> make_consts(const pflbm_config &c) {
     return k;
 }
 
+// ------------------------------------------------------------- closure MLP
+// Eddy-viscosity closure: features x = (Pi_xx, Pi_yy, Pi_zz, Pi_xy, Pi_xz,
+// Pi_yz, phi, |grad phi|), normalised x' = (x - mean) * inv_scale;
+// a1 = W1 x' + b1, h1 = SiLU(a1); a2 = W2 h1 + b2, h2 = SiLU(a2);
+// z = w3 . h2 + b3; nu_t = out_scale * softplus(z).
+// Parameter vector (1377): W1[32][8], b1[32], W2[32][32], b2[32], w3[32], b3.
+constexpr int kIn = 8, kH = 32;
+constexpr int kNumParams = kH * kIn + kH + kH * kH + kH + kH + 1;
+
+struct Mlp {
+    std::vector<double> p = std::vector<double>(kNumParams, 0.0);
+    double mean[kIn] = {0}, inv_scale[kIn] = {1, 1, 1, 1, 1, 1, 1, 1}, out_scale = 0.0;
+    const double *W1() const { return p.data(); }
+    const double *b1() const { return p.data() + kH * kIn; }
+    const double *W2() const { return b1() + kH; }
+    const double *b2() const { return W2() + kH * kH; }
+    const double *w3() const { return b2() + kH; }
+    double b3() const { return *(w3() + kH); }
+};
+
+inline double silu(double a) { return a / (1.0 + std::exp(-a)); }
+inline double dsilu(double a) {
+    const double s = 1.0 / (1.0 + std::exp(-a));
+    return s * (1.0 + a * (1.0 - s));
+}
+inline double softplus(double z) { return std::fmax(z, 0.0) + std::log1p(std::exp(-std::fabs(z))); }
+inline double dsoftplus(double z) { return 1.0 / (1.0 + std::exp(-z)); }
+
+// Forward; returns nu_t. With grad != null, accumulates d(loss)/d(params)
+// for loss = (nu_t - target)^2 / out_scale^2 (the library's training loss).
+double mlp_eval(const Mlp &m, const double *x, double target, double *grad) {
+    double xn[kIn], a1[kH], h1[kH], a2[kH], h2[kH];
+    for (int k = 0; k < kIn; ++k) xn[k] = (x[k] - m.mean[k]) * m.inv_scale[k];
+    for (int i = 0; i < kH; ++i) {
+        double s = m.b1()[i];
+        for (int k = 0; k < kIn; ++k) s += m.W1()[i * kIn + k] * xn[k];
+        a1[i] = s;
+        h1[i] = silu(s);
+    }
+    double z = m.b3();
+    for (int j = 0; j < kH; ++j) {
+        double s = m.b2()[j];
+        for (int i = 0; i < kH; ++i) s += m.W2()[j * kH + i] * h1[i];
+        a2[j] = s;
+        h2[j] = silu(s);
+        z += m.w3()[j] * h2[j];
+    }
+    const double y = m.out_scale * softplus(z);
+    if (grad) {
+        // d loss / d z with loss = (softplus(z) - target/out_scale)^2
+        const double r = softplus(z) - target / m.out_scale;
+        const double dz = 2.0 * r * dsoftplus(z);
+        double *gW1 = grad, *gb1 = grad + kH * kIn, *gW2 = gb1 + kH, *gb2 = gW2 + kH * kH, *gw3 = gb2 + kH,
+               *gb3 = gw3 + kH;
+        *gb3 += dz;
+        double da2[kH];
+        for (int j = 0; j < kH; ++j) {
+            gw3[j] += dz * h2[j];
+            da2[j] = dz * m.w3()[j] * dsilu(a2[j]);
+            gb2[j] += da2[j];
+            for (int i = 0; i < kH; ++i) gW2[j * kH + i] += da2[j] * h1[i];
+        }
+        for (int i = 0; i < kH; ++i) {
+            double dh = 0.0;
+            for (int j = 0; j < kH; ++j) dh += m.W2()[j * kH + i] * da2[j];
+            const double da1 = dh * dsilu(a1[i]);
+            gb1[i] += da1;
+            for (int k = 0; k < kIn; ++k) gW1[i * kIn + k] += da1 * xn[k];
+        }
+    }
+    return y;
+}
+
 // -------------------------------------------------------------- simulation
 struct OracleBase {
     virtual ~OracleBase() = default;
@@ -223,6 +296,8 @@ struct OracleBase {
     virtual const void *field(int id, int *is_double) const = 0;
     virtual const void *pops(int which, int *is_double) const = 0;
     uint64_t t = 0;
+    Mlp mlp;            // closure network (used when closure_strength != 0)
+    double closure_strength = 0.0;
 };
 
 template <class T>
@@ -459,13 +534,19 @@ struct Oracle final : OracleBase {
             const T fsx = F(PFLBM_FIELD_FFX, i), fsy = F(PFLBM_FIELD_FFY, i), fsz = F(PFLBM_FIELD_FFZ, i);
             const T phi = F(PFLBM_FIELD_PHI, i);
             T omega;
+            T tau_t = T(0);  // eddy-viscosity increment of the closure, in tau units
+            if (closure_strength != 0.0) {
+                const double x[8] = {double(pxx), double(pyy), double(pzz), double(pxy), double(pxz), double(pyz),
+                                     double(phi), double(F(PFLBM_FIELD_IND, i))};
+                tau_t = T(3) * static_cast<T>(closure_strength * mlp_eval(mlp, x, 0.0, nullptr));
+            }
             if (jet) {
-                const T tau_phi = (T(1) - phi) * K.tau_water + phi * K.tau_oil;
+                const T tau_phi = (T(1) - phi) * K.tau_water + phi * K.tau_oil + tau_t;
                 const T r = K.sponge_ramp(z);
                 const T tau_eff = tau_phi + r * (K.tau_zmax(phi) - tau_phi);
                 omega = T(1) / tau_eff;
             } else {
-                omega = K.omega_ref;
+                omega = tau_t == T(0) ? K.omega_ref : T(1) / (T(1) / K.omega_ref + tau_t);
             }
             const T omco = T(1) - omega;
             const T uu = T(1.5) * (ux * ux + uy * uy + uz * uz);
@@ -718,6 +799,31 @@ void ora_velocity_set(int vs, int *cx, int *cy, int *cz, float *w) {
     Lattice<float> L(vs);
     for (int q = 0; q < L.Q; ++q) { cx[q] = kCX[q]; cy[q] = kCY[q]; cz[q] = kCZ[q]; w[q] = L.w[q]; }
 }
+// ---- closure MLP hooks ---------------------------------------------------
+int ora_mlp_num_params(void) { return kNumParams; }
+
+// Forward (and, with grad != null, the summed gradient of the training loss)
+// over n samples x[n][8] with targets t[n]; out[n] = nu_t.
+void ora_mlp_eval(const double *params, const double *mean, const double *inv_scale, double out_scale, const double *x,
+                  const double *t, int n, double *out, double *grad) {
+    Mlp m;
+    m.p.assign(params, params + kNumParams);
+    for (int k = 0; k < kIn; ++k) { m.mean[k] = mean[k]; m.inv_scale[k] = inv_scale[k]; }
+    m.out_scale = out_scale;
+    if (grad) std::fill(grad, grad + kNumParams, 0.0);
+    for (int i = 0; i < n; ++i) out[i] = mlp_eval(m, x + 8 * i, t ? t[i] : 0.0, grad);
+}
+
+// Attaches a closure network to an oracle simulation (strength 0 detaches).
+void ora_set_closure(void *h, const double *params, const double *mean, const double *inv_scale, double out_scale,
+                     double strength) {
+    OracleBase *o = static_cast<OracleBase *>(h);
+    o->mlp.p.assign(params, params + kNumParams);
+    for (int k = 0; k < kIn; ++k) { o->mlp.mean[k] = mean[k]; o->mlp.inv_scale[k] = inv_scale[k]; }
+    o->mlp.out_scale = out_scale;
+    o->closure_strength = strength;
+}
+
 uint32_t ora_hash32(uint32_t x) { return hash32(x); }
 float ora_white_noise(uint32_t salt, uint32_t x, uint32_t y, uint32_t t) { return white_noise(salt, x, y, t); }
 float ora_uniform_noise(uint32_t seed, uint32_t x, uint32_t y, uint32_t t) { return uniform_noise(seed, x, y, t); }

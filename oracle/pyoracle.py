@@ -66,6 +66,10 @@ def load() -> ctypes.CDLL:
     lib.ora_sponge_ramp.argtypes = [vp, u32]
     lib.ora_sponge_ramp.restype = ctypes.c_float
     lib.ora_relaxation.argtypes = [vp, fp]
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.ora_mlp_num_params.restype = i32
+    lib.ora_mlp_eval.argtypes = [vp, vp, vp, ctypes.c_double, vp, vp, i32, vp, vp]
+    lib.ora_set_closure.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double]
     _LIB = lib
     return lib
 
@@ -105,6 +109,12 @@ class OracleSim:
         if self.lib.ora_get_field(self._h, FIELDS.index(name), a.ctypes.data, a.size) != 0:
             raise ValueError(f"field {name} not available in the oracle")
         return a
+
+    def set_closure(self, params, mean, inv_scale, out_scale, strength=1.0):
+        p = np.ascontiguousarray(params, np.float64)
+        mu = np.ascontiguousarray(mean, np.float64)
+        sc = np.ascontiguousarray(inv_scale, np.float64)
+        self.lib.ora_set_closure(self._h, p.ctypes.data, mu.ctypes.data, sc.ctypes.data, float(out_scale), float(strength))
 
     def close(self):
         if self._h:
@@ -185,3 +195,19 @@ def relaxation(config) -> np.ndarray:
     out = (ctypes.c_float * 7)()
     load().ora_relaxation(ctypes.byref(config), out)
     return np.array(out, np.float32)
+
+
+def mlp_eval(params, mean, inv_scale, out_scale, x, targets=None, with_grad=False):
+    """FP64 forward (and summed training-loss gradient) of the closure MLP."""
+    lib = load()
+    p = np.ascontiguousarray(params, np.float64)
+    mu = np.ascontiguousarray(mean, np.float64)
+    sc = np.ascontiguousarray(inv_scale, np.float64)
+    xx = np.ascontiguousarray(x, np.float64).reshape(-1, 8)
+    n = xx.shape[0]
+    t = np.ascontiguousarray(targets if targets is not None else np.zeros(n), np.float64)
+    out = np.empty(n, np.float64)
+    g = np.empty(lib.ora_mlp_num_params(), np.float64) if with_grad else None
+    lib.ora_mlp_eval(p.ctypes.data, mu.ctypes.data, sc.ctypes.data, float(out_scale), xx.ctypes.data, t.ctypes.data, n,
+                     out.ctypes.data, g.ctypes.data if g is not None else None)
+    return (out, g) if with_grad else out

@@ -40,11 +40,59 @@
 
 namespace pflbm {
 
+// Resident CTAs per SM the collide kernels are compiled for (sets the
+// register cap: 65536 / (256 * this)).
+#ifndef PFLBM_COLLIDE_MIN_BLOCKS
+#define PFLBM_COLLIDE_MIN_BLOCKS 2
+#endif
+
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 constexpr int PX = TX + 4, PY = TY + 4;  // phi tile + halo 2
 constexpr int NX_ = TX + 2, NY_ = TY + 2;  // normal tile + halo 1
 
-enum Mode { MODE_STEP = 0, MODE_STEP_AVG = 1, MODE_ANALYSIS = 2 };
+enum Mode { MODE_STEP = 0, MODE_STEP_AVG = 1, MODE_ANALYSIS = 2, MODE_STEP_CLOSURE = 3 };
+
+// ------------------------------------------------------------ closure MLP
+// Eddy-viscosity network of the learned closure: x = (Pi_xx, Pi_yy, Pi_zz,
+// Pi_xy, Pi_xz, Pi_yz, phi, |grad phi|) -> 32 -> 32 -> 1, SiLU, softplus.
+// Device blob layout (floats): W1[32][8], b1[32], W2[32][32], b2[32], w3[32],
+// b3, mean[8], inv_scale[8], out_scale, strength.
+constexpr int kMlpIn = 8, kMlpH = 32;
+constexpr int kMlpParams = kMlpH * kMlpIn + kMlpH + kMlpH * kMlpH + kMlpH + kMlpH + 1;  // 1377
+constexpr int kMlpBlob = kMlpParams + 2 * kMlpIn + 2;                                   // 1395
+constexpr int kMlpW1 = 0, kMlpB1 = kMlpH * kMlpIn, kMlpW2 = kMlpB1 + kMlpH, kMlpB2 = kMlpW2 + kMlpH * kMlpH,
+              kMlpW3 = kMlpB2 + kMlpH, kMlpB3 = kMlpW3 + kMlpH, kMlpMean = kMlpParams,
+              kMlpInvScale = kMlpMean + kMlpIn, kMlpOutScale = kMlpInvScale + kMlpIn, kMlpStrength = kMlpOutScale + 1;
+
+template <class T>
+__device__ __forceinline__ T silu_d(T a) { return a / (T(1) + exp(-a)); }
+template <class T>
+__device__ __forceinline__ T softplus_d(T z) { return (z > T(0) ? z : T(0)) + log1p(exp(-fabs(z))); }
+
+// nu_t of one node (no strength factor); w points at the blob (shared memory).
+template <class T>
+__device__ __forceinline__ T mlp_nu_t(const float *w, const T (&x)[kMlpIn]) {
+    T xn[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) xn[k] = (x[k] - T(w[kMlpMean + k])) * T(w[kMlpInvScale + k]);
+    T h1[kMlpH];
+#pragma unroll
+    for (int i = 0; i < kMlpH; ++i) {
+        T s = T(w[kMlpB1 + i]);
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) s += T(w[kMlpW1 + i * kMlpIn + k]) * xn[k];
+        h1[i] = silu_d<T>(s);
+    }
+    T z = T(w[kMlpB3]);
+#pragma unroll 4
+    for (int j = 0; j < kMlpH; ++j) {
+        T s = T(w[kMlpB2 + j]);
+#pragma unroll
+        for (int i = 0; i < kMlpH; ++i) s += T(w[kMlpW2 + j * kMlpH + i]) * h1[i];
+        z += T(w[kMlpW3 + j]) * silu_d<T>(s);
+    }
+    return T(w[kMlpOutScale]) * softplus_d<T>(z);
+}
 
 // -------------------------------------------------------------- noise
 // Counter hash and Box-Muller of src/BoundaryConditions.cuh:172-213.
@@ -152,7 +200,8 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
                                              uint32_t t, const typename Store<S>::T (&pop)[QQ],
                                              typename Store<S>::T phi, typename Store<S>::T n_x,
                                              typename Store<S>::T n_y, typename Store<S>::T n_z,
-                                             typename Store<S>::T ind, typename Store<S>::T curvature) {
+                                             typename Store<S>::T ind, typename Store<S>::T curvature,
+                                             const float *s_mlp = nullptr) {
     using T = typename Store<S>::T;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N, plane = p.plane;
@@ -163,17 +212,23 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
     // moments (src/lbm.cu:33-128)
     const Macro<T> m = moments<QQ, T>(pop, fx, fy, fz);
 
+    // learned eddy-viscosity increment, in units of tau (tau = 1/2 + 3 nu)
+    T tau_t = T(0);
+    if constexpr (MODE == MODE_STEP_CLOSURE) {
+        const T feat[kMlpIn] = {m.pxx, m.pyy, m.pzz, m.pxy, m.pxz, m.pyz, phi, ind};
+        tau_t = T(3) * (T(s_mlp[kMlpStrength]) * mlp_nu_t<T>(s_mlp, feat));
+    }
     // relaxation (src/lbm.cu:158-170)
     T omega;
     if constexpr (JET) {
-        const T tau_phi = (T(1) - phi) * p.tau_water + phi * p.tau_oil;
+        const T tau_phi = (T(1) - phi) * p.tau_water + phi * p.tau_oil + tau_t;
         const T r = sponge_ramp<T>(p, z);
         const T visc_local = (T(1) - phi) * p.visc_water + phi * p.visc_oil;
         const T tau_zmax = T(0.5) + T(3) * (visc_local * p.kgain1);
         const T tau_eff = tau_phi + r * (tau_zmax - tau_phi);
         omega = T(1) / tau_eff;
     } else {
-        omega = p.omega_ref;
+        omega = tau_t == T(0) ? p.omega_ref : T(1) / (T(1) / p.omega_ref + tau_t);
     }
     const CollideCtx<T> k = make_ctx<QQ, T>(m, fx, fy, fz, T(1) - omega);
 
@@ -321,7 +376,8 @@ struct CollideSmem {
 template <int QQ, bool JET, class S, int MODE>
 __device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> &p,
                                              const StepBuffers<S, typename Store<S>::T> &b, int x0, int y0, int zb,
-                                             int ze, CollideSmem<typename Store<S>::T> &sm) {
+                                             int ze, CollideSmem<typename Store<S>::T> &sm,
+                                             const float *s_mlp = nullptr) {
     using T = typename Store<S>::T;
     auto &s_phi = sm.phi;
     auto &s_n = sm.n;
@@ -412,16 +468,22 @@ __device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> 
         const T curvature = T(3) * (scx + scy + scz);
         const T n_x = nv(0, 0, 0, 0), n_y = nv(1, 0, 0, 0), n_z = nv(2, 0, 0, 0), ind = nv(3, 0, 0, 0);
         const T phi = s_phi[z % 3][ty + 2][tx + 2];
-        collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature);
+        collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature, s_mlp);
     }
 }
 
 template <int QQ, bool JET, class S, int MODE>
-__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : 2))
+__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : PFLBM_COLLIDE_MIN_BLOCKS))
     k_collide(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b) {
     __shared__ CollideSmem<typename Store<S>::T> sm;
+    __shared__ float s_mlp[MODE == MODE_STEP_CLOSURE ? kMlpBlob : 1];
+    if constexpr (MODE == MODE_STEP_CLOSURE) {
+        for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpBlob; i += NT) s_mlp[i] = b.mlp[i];
+        __syncthreads();
+    }
     const int zb = 1 + blockIdx.z * p.zchunk;
-    collide_tile<QQ, JET, S, MODE>(p, b, blockIdx.x * TX, blockIdx.y * TY, zb, min(zb + p.zchunk, int(p.nz) - 1), sm);
+    collide_tile<QQ, JET, S, MODE>(p, b, blockIdx.x * TX, blockIdx.y * TY, zb, min(zb + p.zchunk, int(p.nz) - 1), sm,
+                                   s_mlp);
 }
 
 // -------------------------------------------------------------- k_phase

@@ -49,7 +49,7 @@ struct TmaLayout {
 };
 
 template <int QQ, bool JET, class S, int MODE>
-__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : 2))
+__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : PFLBM_COLLIDE_MIN_BLOCKS))
     k_collide_tma(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b,
                   const __grid_constant__ CUtensorMap fmap, const __grid_constant__ CUtensorMap phimap) {
     using T = typename Store<S>::T;

@@ -53,59 +53,50 @@ struct Macro {
     T pxx, pyy, pzz, pxy, pxz, pyz;  // deviatoric non-equilibrium second moment
 };
 
-// (+c member) - (-c member) accumulation over opposite pairs in ascending
-// order: the summation order of the velocity sums of src/lbm.cu:62-73.
-template <int QQ, class T>
-__device__ __forceinline__ T pair_sum(const T (&f)[QQ], const int *c) {
-    T s = T(0);
-    bool first = true;
-#pragma unroll
-    for (int q = 1; q < QQ; q += 2) {
-        if (c[q] != 0) {
-            const int qp = c[q] > 0 ? q : q + 1;
-            const int qm = c[q] > 0 ? q + 1 : q;
-            if (first) {
-                s = f[qp] - f[qm];
-                first = false;
-            } else {
-                s = s + f[qp];
-                s = s - f[qm];
-            }
-        }
-    }
-    return s;
-}
-
-// Moments of src/lbm.cu:33-128 from the shifted populations f' = f - w.
+// Moments of src/lbm.cu:33-128 from the shifted populations f' = f - w,
+// through the sums s_k = f_(2k-1) + f_(2k) and differences d_k = f_(2k-1) -
+// f_(2k) of the opposite pairs: first moments are sums of d_k, second
+// moments sums of s_k (c_a c_b is the same for q and its opposite).
 template <int QQ, class T>
 __device__ __forceinline__ Macro<T> moments(const T (&f)[QQ], T fx, T fy, T fz) {
-    Macro<T> m;
-    T rho = T(0);
+    constexpr int NP = (QQ - 1) / 2;
+    T sp[NP], dp[NP];
 #pragma unroll
-    for (int q = 0; q < QQ; ++q) rho += f[q];
+    for (int k = 0; k < NP; ++k) {
+        sp[k] = f[2 * k + 1] + f[2 * k + 2];
+        dp[k] = f[2 * k + 1] - f[2 * k + 2];
+    }
+    Macro<T> m;
+    T rho = f[0];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) rho += sp[k];
     rho += T(1);
+    T jx = T(0), jy = T(0), jz = T(0), mxx = T(0), myy = T(0), mzz = T(0), mxy = T(0), mxz = T(0), myz = T(0);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int q = 2 * k + 1;
+        const int cx = kCX[q], cy = kCY[q], cz = kCZ[q];
+        if (cx > 0) jx += dp[k];
+        if (cx < 0) jx -= dp[k];
+        if (cy > 0) jy += dp[k];
+        if (cy < 0) jy -= dp[k];
+        if (cz > 0) jz += dp[k];
+        if (cz < 0) jz -= dp[k];
+        if (cx != 0) mxx += sp[k];
+        if (cy != 0) myy += sp[k];
+        if (cz != 0) mzz += sp[k];
+        if (cx * cy > 0) mxy += sp[k];
+        if (cx * cy < 0) mxy -= sp[k];
+        if (cx * cz > 0) mxz += sp[k];
+        if (cx * cz < 0) mxz -= sp[k];
+        if (cy * cz > 0) myz += sp[k];
+        if (cy * cz < 0) myz -= sp[k];
+    }
     const T inv = T(1) / rho;
-    T ux = inv * pair_sum<QQ, T>(f, kCX);
-    T uy = inv * pair_sum<QQ, T>(f, kCY);
-    T uz = inv * pair_sum<QQ, T>(f, kCZ);
+    T ux = inv * jx, uy = inv * jy, uz = inv * jz;
     ux += fx * T(0.5) * inv;
     uy += fy * T(0.5) * inv;
     uz += fz * T(0.5) * inv;
-    // raw second moments of f'
-    T mxx = T(0), myy = T(0), mzz = T(0), mxy = T(0), mxz = T(0), myz = T(0);
-#pragma unroll
-    for (int q = 1; q < QQ; ++q) {
-        const int cx = kCX[q], cy = kCY[q], cz = kCZ[q];
-        if (cx != 0) mxx += f[q];
-        if (cy != 0) myy += f[q];
-        if (cz != 0) mzz += f[q];
-        if (cx * cy > 0) mxy += f[q];
-        if (cx * cy < 0) mxy -= f[q];
-        if (cx * cz > 0) mxz += f[q];
-        if (cx * cz < 0) mxz -= f[q];
-        if (cy * cz > 0) myz += f[q];
-        if (cy * cz < 0) myz -= f[q];
-    }
     T pxx = mxx - rho * ux * ux + ux * fx;
     T pyy = myy - rho * uy * uy + uy * fy;
     T pzz = mzz - rho * uz * uz + uz * fz;
@@ -122,16 +113,20 @@ __device__ __forceinline__ Macro<T> moments(const T (&f)[QQ], T fx, T fy, T fz) 
     return m;
 }
 
-// Per-node quantities shared by every pair of the collision.
+// Per-node quantities shared by every pair of the collision. Factors that
+// depend only on the weight class (rest, axis, face diagonal, body diagonal)
+// are formed once per node.
 template <class T>
 struct CollideCtx {
     T rho, ux, uy, uz, fx, fy, fz;
     T pxx, pyy, pzz, pxy, pxz, pyz;
-    T omco;       // 1 - omega
-    T A;          // 1 - uu, uu = 1.5 |u|^2
-    T uu;
-    T uF;         // u . F
-    T b1, b2, b3, b4, b5, b6, b7;  // third-order Hermite contractions (D3Q27)
+    T omco;        // 1 - omega
+    T A;           // 1 - uu, uu = 1.5 |u|^2
+    T uF;          // u . F
+    T u3x, u3y, u3z;  // 3 u
+    T wr[4];       // w_class * rho
+    T ow[4];       // (1 - omega) * 4.5 * w_class
+    T h1, h2, h3, h4, h5, h6, h7;  // third-order Hermite contractions (D3Q27)
 };
 
 template <int QQ, class T>
@@ -141,19 +136,29 @@ __device__ __forceinline__ CollideCtx<T> make_ctx(const Macro<T> &m, T fx, T fy,
     k.fx = fx; k.fy = fy; k.fz = fz;
     k.pxx = m.pxx; k.pyy = m.pyy; k.pzz = m.pzz; k.pxy = m.pxy; k.pxz = m.pxz; k.pyz = m.pyz;
     k.omco = omco;
-    k.uu = T(1.5) * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
-    k.A = T(1) - k.uu;
+    k.A = T(1) - T(1.5) * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
     k.uF = m.ux * fx + m.uy * fy + m.uz * fz;
+    k.u3x = T(3) * m.ux;
+    k.u3y = T(3) * m.uy;
+    k.u3z = T(3) * m.uz;
+    const double wc[4] = {Weights<QQ>::w0, Weights<QQ>::w1, Weights<QQ>::w2, Weights<QQ>::w3};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        k.wr[c] = static_cast<T>(wc[c]) * m.rho;
+        k.ow[c] = omco * static_cast<T>(4.5 * wc[c]);
+    }
     if constexpr (QQ == 27) {
-        k.b1 = m.pxx * m.uy + T(2) * m.ux * m.pxy;
-        k.b2 = m.pxx * m.uz + T(2) * m.ux * m.pxz;
-        k.b3 = m.pyy * m.ux + T(2) * m.uy * m.pxy;
-        k.b4 = m.pyy * m.uz + T(2) * m.uy * m.pyz;
-        k.b5 = m.pzz * m.ux + T(2) * m.uz * m.pxz;
-        k.b6 = m.pzz * m.uy + T(2) * m.uz * m.pyz;
-        k.b7 = m.ux * m.pyz + m.uy * m.pxz + m.uz * m.pxy;
+        // b_i of D3Q27.cuh:180-189; the coefficients 3 (c_a^2 c_b - cs2 c_b)
+        // are the integers 2 c_b (c_a != 0) or -c_b (c_a == 0)
+        k.h1 = m.pxx * m.uy + T(2) * m.ux * m.pxy;
+        k.h2 = m.pxx * m.uz + T(2) * m.ux * m.pxz;
+        k.h3 = m.pyy * m.ux + T(2) * m.uy * m.pxy;
+        k.h4 = m.pyy * m.uz + T(2) * m.uy * m.pyz;
+        k.h5 = m.pzz * m.ux + T(2) * m.uz * m.pxz;
+        k.h6 = m.pzz * m.uy + T(2) * m.uz * m.pyz;
+        k.h7 = T(6) * (m.ux * m.pyz + m.uy * m.pxz + m.uz * m.pxy);
     } else {
-        k.b1 = k.b2 = k.b3 = k.b4 = k.b5 = k.b6 = k.b7 = T(0);
+        k.h1 = k.h2 = k.h3 = k.h4 = k.h5 = k.h6 = k.h7 = T(0);
     }
     return k;
 }
@@ -169,67 +174,72 @@ __device__ __forceinline__ T cdot(int cx, int cy, int cz, T vx, T vy, T vz) {
     return s;
 }
 
-// c . Pi . c for a trace-free Pi.
+// c . Pi . c for a trace-free Pi (the body-diagonal directions use
+// pxx + pyy + pzz = 0).
 template <class T>
 __device__ __forceinline__ T cpic(int cx, int cy, int cz, const CollideCtx<T> &k) {
-    T s = T(0);
-    if (cx != 0) s += k.pxx;
-    if (cy != 0) s += k.pyy;
-    if (cz != 0) s += k.pzz;
+    const int nnz = (cx != 0) + (cy != 0) + (cz != 0);
     T o = T(0);
-    if (cx * cy != 0) o += (cx * cy > 0) ? k.pxy : -k.pxy;
-    if (cx * cz != 0) o += (cx * cz > 0) ? k.pxz : -k.pxz;
-    if (cy * cz != 0) o += (cy * cz > 0) ? k.pyz : -k.pyz;
-    return s + T(2) * o;
+    bool first = true;
+    auto add = [&](int sgn, T v) {
+        if (first) { o = sgn > 0 ? v : -v; first = false; }
+        else o = sgn > 0 ? o + v : o - v;
+    };
+    if (cx * cy != 0) add(cx * cy, k.pxy);
+    if (cx * cz != 0) add(cx * cz, k.pxz);
+    if (cy * cz != 0) add(cy * cz, k.pyz);
+    if (nnz == 1) return cx != 0 ? k.pxx : (cy != 0 ? k.pyy : k.pzz);
+    if (nnz == 3) return T(2) * o;
+    const T d = cx == 0 ? (k.pyy + k.pzz) : (cy == 0 ? (k.pxx + k.pzz) : (k.pxx + k.pyy));
+    return d + T(2) * o;
 }
 
-// Third-order Hermite part of D3Q27.cuh:180-189 (odd in c), without the
-// (w*4.5) prefactor. The (c^3 - c) terms vanish identically for c in {-1,0,1}.
+// 3 x (third-order Hermite part of D3Q27.cuh:180-189), odd in c: sum of
+// integer multiples of h1..h7. The (c^3 - c) terms vanish for c in {-1,0,1}.
 template <class T>
 __device__ __forceinline__ T hermite3(int cx, int cy, int cz, const CollideCtx<T> &k) {
-    const double cs2 = 1.0 / 3.0;
-    const T a1 = static_cast<T>(cx * cx * cy - cs2 * cy);
-    const T a2 = static_cast<T>(cx * cx * cz - cs2 * cz);
-    const T a3 = static_cast<T>(cx * cy * cy - cs2 * cx);
-    const T a4 = static_cast<T>(cy * cy * cz - cs2 * cz);
-    const T a5 = static_cast<T>(cx * cz * cz - cs2 * cx);
-    const T a6 = static_cast<T>(cy * cz * cz - cs2 * cy);
+    // 3 (cx^2 cy - cs2 cy) = cy (3 cx^2 - 1), etc.
+    const int a1 = cy * (3 * cx * cx - 1), a2 = cz * (3 * cx * cx - 1), a3 = cx * (3 * cy * cy - 1);
+    const int a4 = cz * (3 * cy * cy - 1), a5 = cx * (3 * cz * cz - 1), a6 = cy * (3 * cz * cz - 1);
     T s = T(0);
-    if (cy != 0) s += a1 * k.b1;
-    if (cz != 0) s += a2 * k.b2;
-    if (cx != 0) s += a3 * k.b3;
-    if (cz != 0) s += a4 * k.b4;
-    if (cx != 0) s += a5 * k.b5;
-    if (cy != 0) s += a6 * k.b6;
-    s = T(3) * s;
-    if (cx * cy * cz != 0) s += T(6 * cx * cy * cz) * k.b7;
+    bool first = true;
+    auto add = [&](int a, T v) {
+        if (a == 0) return;
+        const T term = (a == 2 || a == -2) ? T(2) * v : v;
+        if (first) { s = a > 0 ? term : -term; first = false; }
+        else s = a > 0 ? s + term : s - term;
+    };
+    add(a1, k.h1); add(a2, k.h2); add(a3, k.h3); add(a4, k.h4); add(a5, k.h5); add(a6, k.h6);
+    if (cx * cy * cz != 0) {
+        if (first) { s = cx * cy * cz > 0 ? k.h7 : -k.h7; }
+        else s = cx * cy * cz > 0 ? s + k.h7 : s - k.h7;
+    }
     return s;
 }
 
+__host__ __device__ constexpr int weight_class(int q) { return q == 0 ? 0 : (q <= 6 ? 1 : (q <= 18 ? 2 : 3)); }
+
 // Post-collision shifted populations of the pair (q, q+1), q odd:
-// feq + (1-omega) fneq + F/2 of src/lbm.cu:191-206.
+// feq + (1-omega) fneq + F/2 of src/lbm.cu:191-206, as E + O and E - O.
 template <int QQ, class T>
 __device__ __forceinline__ void collide_pair(int q, const CollideCtx<T> &k, T &out_q, T &out_qbar) {
     const int cx = kCX[q], cy = kCY[q], cz = kCZ[q];
-    const T w = static_cast<T>(weight<QQ>(q));
-    const T cu = T(3) * cdot<T>(cx, cy, cz, k.ux, k.uy, k.uz);
+    const int cl = weight_class(q);
+    const double wd = weight<QQ>(q);
+    const T w = static_cast<T>(wd);
+    const T hw = static_cast<T>(1.5 * wd);
+    const T cu = cdot<T>(cx, cy, cz, k.u3x, k.u3y, k.u3z);
     const T cF = cdot<T>(cx, cy, cz, k.fx, k.fy, k.fz);
-    const T wrho = w * k.rho;
-    // even parts
-    const T feq_e = wrho * (k.A + T(0.5) * cu * cu) - w;
-    const T fneq_e = (w * T(4.5)) * cpic<T>(cx, cy, cz, k);
-    const T frc_e = (T(3) * w) * (cu * cF - k.uF);
-    // odd parts
-    T feq_o;
+    // even: w rho (1 - uu + cu^2/2) - w + (1-omega) 4.5 w c.Pi.c + 1.5 w (cu cF - u.F)
+    const T E = k.wr[cl] * (k.A + T(0.5) * cu * cu) - w + k.ow[cl] * cpic<T>(cx, cy, cz, k) + hw * (cu * cF - k.uF);
+    // odd: w rho cu (1 - uu + cu^2/6) [D3Q27] + 1.5 w cF + (1-omega) 4.5 w H3
+    T O;
     if constexpr (QQ == 27) {
-        feq_o = wrho * cu * (k.A + static_cast<T>(1.0 / 6.0) * cu * cu);
+        O = k.wr[cl] * cu * (k.A + static_cast<T>(1.0 / 6.0) * cu * cu) + hw * cF +
+            k.ow[cl] * hermite3<T>(cx, cy, cz, k);
     } else {
-        feq_o = wrho * cu;
+        O = k.wr[cl] * cu + hw * cF;
     }
-    const T frc_o = (T(3) * w) * cF;
-    T E = feq_e + k.omco * fneq_e + T(0.5) * frc_e;
-    T O = feq_o + T(0.5) * frc_o;
-    if constexpr (QQ == 27) O += k.omco * ((w * T(4.5)) * hermite3<T>(cx, cy, cz, k));
     out_q = E + O;
     out_qbar = E - O;
 }
@@ -237,7 +247,7 @@ __device__ __forceinline__ void collide_pair(int q, const CollideCtx<T> &k, T &o
 template <int QQ, class T>
 __device__ __forceinline__ T collide_rest(const CollideCtx<T> &k) {
     const T w = static_cast<T>(weight<QQ>(0));
-    return w * k.rho * k.A - w + T(0.5) * ((T(-3) * w) * k.uF);
+    return k.wr[0] * k.A - w - static_cast<T>(1.5 * weight<QQ>(0)) * k.uF;
 }
 
 // Equilibrium only (no non-equilibrium, no force) for direction q:

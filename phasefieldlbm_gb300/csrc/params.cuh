@@ -91,6 +91,7 @@ struct StepBuffers {
     T *avg;            // 10*N derived averages (or null)
     T *macro;          // 18*N analysis output (or null)
     unsigned int *err; // device error flag
+    const float *mlp;  // closure network blob (MODE_STEP_CLOSURE)
 };
 
 // Order of the macroscopic arrays in the analysis cache; equals
