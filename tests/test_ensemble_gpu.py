@@ -35,7 +35,7 @@ def test_boxes_match_single_runs(pflbm, vs):
         with pflbm.Simulation(c) as s:
             s.step(steps)
             for f in FIELDS:
-                tol = 1e-6 if f in ("rho", "phi") else 1e-4
+                tol = 1e-6 if f in ("rho", "phi") else 1e-3  # u: spurious currents ~1e-6
                 assert rel_l2(got[k][f], s.get_field(f)) <= tol, (k, f)
 
 
