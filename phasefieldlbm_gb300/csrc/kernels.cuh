@@ -46,7 +46,15 @@ namespace pflbm {
 #define PFLBM_COLLIDE_MIN_BLOCKS 2
 #endif
 
-constexpr int TX = 32, TY = 8, NT = TX * TY;
+// Column tile of the collide kernels (x fastest; TX a multiple of 32).
+#ifndef PFLBM_TILE_X
+#define PFLBM_TILE_X 32
+#endif
+#ifndef PFLBM_TILE_Y
+#define PFLBM_TILE_Y 8
+#endif
+
+constexpr int TX = PFLBM_TILE_X, TY = PFLBM_TILE_Y, NT = TX * TY;
 constexpr int PX = TX + 4, PY = TY + 4;  // phi tile + halo 2
 constexpr int NX_ = TX + 2, NY_ = TY + 2;  // normal tile + halo 1
 
