@@ -22,6 +22,7 @@
 
 #include "../../include/pflbm.h"
 #include "engine.h"
+#include "tile.h"
 
 using pflbm::Engine;
 using pflbm::HostParams;
@@ -175,7 +176,7 @@ int pick_zchunk(const pflbm_config &c, int device) {
     }
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const int ctas_xy = int((c.nx + 31) / 32) * int((c.ny + 7) / 8);
+    const int ctas_xy = int((c.nx + pflbm::kTileX - 1) / pflbm::kTileX) * int((c.ny + pflbm::kTileY - 1) / pflbm::kTileY);
     const int nzi = int(c.nz) - 2;
     int chunks = (8 * sms + ctas_xy - 1) / ctas_xy;
     if (chunks < 1) chunks = 1;

@@ -37,22 +37,9 @@
 
 #include "lattice.cuh"
 #include "params.cuh"
+#include "tile.h"
 
 namespace pflbm {
-
-// Resident CTAs per SM the collide kernels are compiled for (sets the
-// register cap: 65536 / (256 * this)).
-#ifndef PFLBM_COLLIDE_MIN_BLOCKS
-#define PFLBM_COLLIDE_MIN_BLOCKS 2
-#endif
-
-// Column tile of the collide kernels (x fastest; TX a multiple of 32).
-#ifndef PFLBM_TILE_X
-#define PFLBM_TILE_X 32
-#endif
-#ifndef PFLBM_TILE_Y
-#define PFLBM_TILE_Y 8
-#endif
 
 constexpr int TX = PFLBM_TILE_X, TY = PFLBM_TILE_Y, NT = TX * TY;
 constexpr int PX = TX + 4, PY = TY + 4;  // phi tile + halo 2

@@ -36,16 +36,23 @@ struct TmaLayout {
     static constexpr int PXO = 4;                      // phi is FP32 or FP64
     static constexpr int PBW = TX + 2 * PXO;           // 40
     static constexpr int PBH = TY + 4;                 // 12
+    // bytes the TMA unit writes per box / phi plane
     static constexpr size_t box_bytes = size_t(TY) * BW * sizeof(S);
-    static constexpr size_t stage_bytes = size_t(QQ) * box_bytes;
-    static constexpr size_t phi_slot_bytes = size_t(PBH) * PBW * sizeof(T);
+    static constexpr size_t phi_plane_bytes = size_t(PBH) * PBW * sizeof(T);
+    // shared-memory strides: every TMA destination starts on a 128-byte boundary
+    static constexpr size_t box_stride = align128(box_bytes);
+    static constexpr size_t stage_bytes = size_t(QQ) * box_stride;
+    static constexpr size_t phi_slot_bytes = align128(phi_plane_bytes);
     static constexpr size_t off_f = 0;
     static constexpr size_t off_phi = align128(2 * stage_bytes);
     static constexpr size_t off_n = align128(off_phi + 4 * phi_slot_bytes);
     static constexpr size_t n_bytes = size_t(4) * 4 * NY_ * NX_ * sizeof(T);
     static constexpr size_t off_bar = align128(off_n + n_bytes);
     static constexpr size_t total = off_bar + 128;
-    static constexpr uint32_t tx_bytes = uint32_t(stage_bytes + phi_slot_bytes);
+    static constexpr uint32_t tx_bytes = uint32_t(QQ * box_bytes + phi_plane_bytes);
+    static_assert(box_stride % 128 == 0 && phi_slot_bytes % 128 == 0 && off_phi % 128 == 0, "TMA smem alignment");
+    static_assert((BW * sizeof(S)) % 16 == 0 && (PBW * sizeof(T)) % 16 == 0, "TMA inner box extent");
+    static_assert(BW <= 256 && PBW <= 256 && TY <= 256 && PBH <= 256, "TMA box dimension limit");
 };
 
 template <int QQ, bool JET, class S, int MODE>
@@ -70,17 +77,20 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
     const bool col = (x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2);
     const uint32_t t = b.step_in ? static_cast<uint32_t>(*b.step_in) : b.t_fixed;
 
-    auto phi_at = [&](int slot, int ly, int lx) -> T & { return s_phi[(slot * L::PBH + ly) * L::PBW + lx]; };
+    auto phi_at = [&](int slot, int ly, int lx) -> T & {
+        return *reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(s_phi) + slot * L::phi_slot_bytes +
+                                      (size_t(ly) * L::PBW + lx) * sizeof(T));
+    };
     auto n_at = [&](int c, int slot, int ly, int lx) -> T & { return s_n[((c * 4 + slot) * NY_ + ly) * NX_ + lx]; };
     auto issue = [&](int stage, int zf) {
         // generic-proxy accesses to the recycled slots are ordered before the
         // async-proxy writes by the preceding block barrier and this fence
         fence_proxy_async();
         mbar_arrive_expect_tx(&bar[stage], L::tx_bytes);
-        S *dst = s_f + size_t(stage) * QQ * TY * L::BW;
-#pragma unroll 1
+        unsigned char *dst = reinterpret_cast<unsigned char *>(s_f) + size_t(stage) * L::stage_bytes;
+#pragma unroll
         for (int q = 0; q < QQ; ++q)
-            tma_load_4d(dst + size_t(q) * TY * L::BW, &fmap, &bar[stage], x0 - L::XO, y0 - kCY[q], zf - kCZ[q], q);
+            tma_load_4d(dst + size_t(q) * L::box_stride, &fmap, &bar[stage], x0 - L::XO, y0 - kCY[q], zf - kCZ[q], q);
         tma_load_3d(&phi_at((zf + 2) & 3, 0, 0), &phimap, &bar[stage], x0 - L::PXO, y0 - 2, zf + 2);
     };
 
@@ -166,10 +176,12 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
         const T phi = phi_at(z & 3, ty + 2, tx + L::PXO);
 
         T pop[QQ];
-        const S *sf = s_f + size_t(st) * QQ * TY * L::BW + size_t(ty) * L::BW + tx + L::XO;
+        const unsigned char *sf = reinterpret_cast<const unsigned char *>(s_f) + size_t(st) * L::stage_bytes +
+                                  (size_t(ty) * L::BW + tx + L::XO) * sizeof(S);
 #pragma unroll
         for (int q = 0; q < QQ; ++q)
-            pop[q] = Store<S>::widen(sf[size_t(q) * TY * L::BW - kCX[q]], static_cast<T>(weight<QQ>(q)));
+            pop[q] = Store<S>::widen(*reinterpret_cast<const S *>(sf + size_t(q) * L::box_stride - kCX[q] * int(sizeof(S))),
+                                     static_cast<T>(weight<QQ>(q)));
         collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature);
     }
 }
