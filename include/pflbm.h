@@ -193,6 +193,36 @@ int pflbm_get_field_f64(pflbm_sim *sim, int32_t field_id, double *host_dst, size
  * PFLBM_ERR_DIVERGED when nonfinite > 0 (the diag is still filled). */
 int pflbm_reduce(pflbm_sim *sim, pflbm_diag *out);
 
+/* The reductions of pflbm_reduce over caller-owned device fields, allocating
+ * no device memory. No counterpart in the reference. It is meant for callers
+ * that cannot let a library call cudaMalloc: in-situ analysis hooks inside
+ * another solver's time loop, or host frameworks whose memory pool reserves
+ * the device heap (a cudaMalloc/cudaFree pair would also synchronise the
+ * device in the middle of their pipeline).
+ *
+ * rho, ux, uy, uz, phi: nx*ny*nz float32 device arrays on the calling
+ * thread's current device, laid out as pflbm_get_field writes them (ghost
+ * shell included; only interior nodes are summed). dev_out: a device
+ * pflbm_diag, filled as pflbm_reduce fills it except step = 0; NaN/Inf show
+ * up in dev_out->nonfinite, not in the return code. The kernels are enqueued
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream) and the call
+ * returns without waiting for them.
+ *
+ * Scratch: one row of FP64 partial sums per interior z plane in a fixed
+ * device array of PFLBM_NOALLOC_MAX_PLANES rows (384 KiB) that every GPU
+ * loading the library holds until the process exits. nz - 2 above
+ * PFLBM_NOALLOC_MAX_PLANES is rejected with PFLBM_ERR_INVALID_ARG. All calls
+ * on a device share that array: calls whose kernels overlap on the GPU (on
+ * different streams) race and must be serialised by the caller. Each call
+ * writes every row it reads, so no earlier call's contents leak into a result.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. */
+#define PFLBM_NOALLOC_MAX_PLANES 4096
+int pflbm_reduce_fields_noalloc(const float *rho, const float *ux, const float *uy, const float *uz,
+                                const float *phi, int32_t nx, int32_t ny, int32_t nz, void *stream,
+                                pflbm_diag *dev_out);
+
 /* Writes <dir>/<name><step:06>.bin for each field and <dir>/step_<step:06>.vti
  * that appends them (src/postProcess/PostProcess.cuh:43-261). */
 int pflbm_write_output(pflbm_sim *sim, const char *dir, const int32_t *field_ids, int32_t n_fields);

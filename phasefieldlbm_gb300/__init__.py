@@ -159,6 +159,7 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_get_field": ([vp, i32, vp, sz], ctypes.c_int),
         "pflbm_get_field_f64": ([vp, i32, vp, sz], ctypes.c_int),
         "pflbm_reduce": ([vp, ctypes.POINTER(Diag)], ctypes.c_int),
+        "pflbm_reduce_fields_noalloc": ([vp, vp, vp, vp, vp, i32, i32, i32, vp, vp], ctypes.c_int),
         "pflbm_write_output": ([vp, ctypes.c_char_p, ctypes.POINTER(i32), i32], ctypes.c_int),
         "pflbm_device_bytes": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
         "pflbm_save_checkpoint": ([vp, ctypes.c_char_p], ctypes.c_int),
