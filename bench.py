@@ -18,6 +18,21 @@ are far larger than the 129 MB L2, so no flush is needed between steps.
 has no CPU path, and its CUDA build is a GPU baseline, reported separately.
 Multi-GPU runs are independent replicas (one simulation per GPU, no
 exchange); scaling is weak.
+
+  python bench.py --study precision [--checkpoints 500,1000,...]
+
+prints the storage-precision study (FP32/FP16/BF16 storage against the FP64
+path on the 128x128x512 D3Q19 jet, MLUPS on 256x256x1024) instead.
+
+  python bench.py --study closure
+
+trains the learned closure on filtered 256x256x1024 snapshots and judges it
+against plain constant-tau on the 128x128x512 grid (time-averaged u_z, phi).
+
+  python bench.py --study ensemble
+
+times the 64-box droplet ensemble (batched, autotuned) against the same boxes
+run sequentially.
 """
 from __future__ import annotations
 
@@ -153,21 +168,33 @@ def cpu_oracle_mlups(cfg, steps: int, warm: int = 1) -> tuple[float, float, int]
     return cfg.nodes * steps / dt / 1e6, dt, os.cpu_count() or 1
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_collide
+# launch from ncu on the 128x128x128 profiling case, scaled to the
+# 128x128x512 workload by the number of interior planes (510 / 126); see
+# profiles/k_collide_tma_jet_d3q27_fp32_128x128x128.md and ..._d3q19_....md.
+NCU_COLLIDE_TRAFFIC = {
+    "jet_d3q27": (250.120960e6 + 199.445248e6) * 510 / 126,
+    "jet_d3q19": (179.785984e6 + 134.822144e6) * 510 / 126,
+}
+
+
 def traffic_for(workload: str):
-    p = ROOT / "profiles" / "traffic.json"
-    if not p.exists():
-        return None
-    try:
-        return json.loads(p.read_text()).get(workload)
-    except (ValueError, OSError):
-        return None
+    v = NCU_COLLIDE_TRAFFIC.get(workload)
+    return {"collide_bytes_per_launch": int(v)} if v else None
 
 
 # ---------------------------------------------------------------- arms
+def workload_config(args):
+    """The bench workload; --nz shortens the jet for profiling captures."""
+    import phasefieldlbm_gb300 as pf
+
+    return pf.preset(args.workload, nz=args.nz) if args.nz else pf.preset(args.workload)
+
+
 def run_gpu(args, ranks: Ranks) -> dict:
     import phasefieldlbm_gb300 as pf
 
-    cfg = pf.preset(args.workload)
+    cfg = workload_config(args)
     cfg.device = ranks.local
     N = cfg.nodes
     q = int(cfg.velocity_set)
@@ -201,7 +228,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
     phase_s = kms[1] / 1e3 / launches
     achieved = ba["collide"] * N / collide_s / 1e9
     step_achieved = ba["total"] * N / ((kms[0] + kms[1]) / 1e3 / launches) / 1e9
-    tr = traffic_for(args.workload)
+    tr = None if args.nz else traffic_for(args.workload)
     roofline = {
         "bound": "hbm", "kernel": "k_collide", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
         "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
@@ -293,7 +320,7 @@ def run_reference(args, ranks: Ranks) -> dict | None:
     import phasefieldlbm_gb300 as pf
     from oracle import pyoracle
 
-    cfg = pf.preset(args.workload)
+    cfg = workload_config(args)
     o = pyoracle.OracleSim(cfg)
     o.step(args.warmup)
     t0 = time.perf_counter()
@@ -314,6 +341,161 @@ def run_reference(args, ranks: Ranks) -> dict | None:
     }
 
 
+def run_precision_study(args) -> dict:
+    """Storage-precision study of the D3Q19 jet: FP32, FP16 and BF16 storage
+    against the FP64 path on the 128x128x512 (D=16) instance, all four runs
+    advanced in lockstep on the GPU and compared at checkpoints (relative L2
+    of rho, of u_z on the centreline x = nx/2, y = ny/2, and of phi), plus
+    the MLUPS of each storage on the 256x256x1024 (D=32) configuration."""
+    import numpy as np
+
+    import phasefieldlbm_gb300 as pf
+
+    def rl2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    names = {"fp64": pf.STORAGE_FP64, "fp32": pf.STORAGE_FP32, "fp16": pf.STORAGE_FP16, "bf16": pf.STORAGE_BF16}
+    checkpoints = [int(c) for c in args.checkpoints.split(",")]
+    sims = {k: pf.Simulation(pf.preset("jet_d3q19", storage=v)) for k, v in names.items()}
+    errors, done = [], 0
+    for cp in checkpoints:
+        for s in sims.values():
+            s.step(cp - done)
+        done = cp
+        c = sims["fp64"].config
+        cx, cy = int(c.nx) // 2, int(c.ny) // 2
+        ref = {f: sims["fp64"].get_field(f, dtype=np.float64) for f in ("rho", "uz", "phi")}
+        row = {"step": cp}
+        for k in ("fp32", "fp16", "bf16"):
+            got = {f: sims[k].get_field(f, dtype=np.float64) for f in ("rho", "uz", "phi")}
+            row[k] = {"rho": rl2(got["rho"], ref["rho"]),
+                      "uz_centreline": rl2(got["uz"][:, cy, cx], ref["uz"][:, cy, cx]),
+                      "uz": rl2(got["uz"], ref["uz"]), "phi": rl2(got["phi"], ref["phi"]),
+                      "phi_mass_drift": float(sims[k].reduce().phi_mass / sims["fp64"].reduce().phi_mass - 1.0)}
+        errors.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    for s in sims.values():
+        s.close()
+    mlups = {}
+    for k in ("fp32", "fp16", "bf16"):
+        c = pf.preset("jet_precision", storage=names[k])
+        with pf.Simulation(c) as s:
+            s.step(50)
+            tot, _ = s.step_profiled(200)
+            mlups[k] = round(c.nodes * 200 / (tot / 1e3) / 1e6, 1)
+    return {"study": "precision", "case": "jet D3Q19+D3Q7, Re=5000, We=500, uniform 5% inflow noise (seed 12345)",
+            "error_grid": "128x128x512, D=16, against the FP64 path", "mlups_grid": "256x256x1024, D=32",
+            "errors": errors, "mlups": mlups}
+
+
+def restrict_filtered(a):
+    """3x3x3 box filter around fine node 2X, sampled at coarse node X."""
+    nz, ny, nx = a.shape
+    acc = np.zeros((nz // 2, ny // 2, nx // 2))
+    for dz in (-1, 0, 1):
+        zi = np.clip(np.arange(nz // 2) * 2 + dz, 0, nz - 1)
+        for dy in (-1, 0, 1):
+            yi = np.clip(np.arange(ny // 2) * 2 + dy, 0, ny - 1)
+            for dx in (-1, 0, 1):
+                xi = np.clip(np.arange(nx // 2) * 2 + dx, 0, nx - 1)
+                acc += a[np.ix_(zi, yi, xi)]
+    return acc / 27.0
+
+
+def run_closure_study(args) -> dict:
+    """Learned closure on the D3Q19 jet at Re = 10000: a 256x256x1024 (D=32)
+    run gives 20 snapshots (every 500 steps) that are box-filtered and
+    restricted to the 128x128x512 (D=16) grid; the MLP is trained on them on
+    the GPU; plain constant-tau and closure runs on the coarse grid are then
+    judged by the relative L2 error of their time-averaged u_z and phi
+    against the filtered time average of the fine run over the same
+    physical time (coarse steps = fine steps / 2)."""
+    import phasefieldlbm_gb300 as pf
+
+    t0 = time.perf_counter()
+    n_snap, every = args.snapshots, args.snapshot_every
+    fine_steps = n_snap * every
+    coarse_steps = fine_steps // 2
+    fine_cfg = pf.preset("jet_closure_fine", flags=pf.FLAG_TIME_AVERAGE)
+    stride = args.sample_stride
+    per_snap = ((fine_cfg.nx // 2 - 3) // stride + 1) * ((fine_cfg.ny // 2 - 3) // stride + 1) * (fine_cfg.nz // 2 - 4)
+    out = {"study": "closure", "fine": "256x256x1024 D=32 Re=10000", "coarse": "128x128x512 D=16 Re=10000",
+           "fine_steps": fine_steps, "coarse_steps": coarse_steps, "snapshots": n_snap, "sample_stride": stride}
+    with pf.Closure(per_snap * n_snap) as cl:
+        with pf.Simulation(fine_cfg) as fine:
+            for k in range(n_snap):
+                fine.step(every)
+                cl.add_snapshot(fine, stride=stride)
+            ref = {f: restrict_filtered(fine.get_field(f)) for f in ("avg_uz", "avg_phi")}
+        out["samples"] = cl.num_samples
+        out["t_fine_s"] = round(time.perf_counter() - t0, 1)
+        cl.init_params(seed=args.seed)
+        loss0 = cl.loss()
+        t1 = time.perf_counter()
+        hist = cl.train(args.train_iters, batch=args.train_batch, lr=args.train_lr, seed=args.seed)
+        out["train"] = {"iterations": args.train_iters, "batch": args.train_batch, "lr": args.train_lr,
+                        "loss_init": loss0, "loss_final": cl.loss(), "minibatch_last": float(hist[-1]),
+                        "seconds": round(time.perf_counter() - t1, 2)}
+        blob = cl.blob
+
+    def coarse_run(strength):
+        c = pf.preset("jet_closure", flags=pf.FLAG_TIME_AVERAGE)
+        with pf.Simulation(c) as s:
+            if strength > 0:
+                s.set_closure(blob, strength)
+            ta = time.perf_counter()
+            s.step(coarse_steps)
+            dt = time.perf_counter() - ta
+            return {f: s.get_field(f).astype(np.float64) for f in ("avg_uz", "avg_phi")}, c.nodes * coarse_steps / dt / 1e6
+
+    def errors(res):
+        sl = (slice(2, -2), slice(2, -2), slice(2, -2))
+        cz, cy, cx = [n // 2 for n in res["avg_uz"].shape]
+        e = {}
+        for f in ("avg_uz", "avg_phi"):
+            a, b = res[f][sl], ref[f][sl]
+            e[f] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            e[f + "_centreline"] = float(np.linalg.norm(res[f][2:-2, cy, cx] - ref[f][2:-2, cy, cx]) /
+                                         np.linalg.norm(ref[f][2:-2, cy, cx]))
+        return e
+
+    runs = {}
+    for name, strength in (("plain", 0.0), ("closure", 1.0)) + tuple(
+            (f"closure_x{s:g}", s) for s in args.extra_strengths):
+        res, mlups = coarse_run(strength)
+        runs[name] = {"strength": strength, "mlups": round(mlups, 1), **errors(res)}
+    out["runs"] = runs
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def run_ensemble_study(args) -> dict:
+    """The batched droplet ensemble: 64 seeded periodic boxes (edges in
+    {32,48,64,80,96}), autotuned, `steps` steps in the persistent
+    graph-captured launches, against the same boxes run one after another as
+    single simulations (each with its own captured graph)."""
+    import phasefieldlbm_gb300 as pf
+
+    steps = args.ensemble_steps
+    cfgs = pf.ensemble_configs(64)
+    total_nodes = sum(c.nodes for c in cfgs)
+    with pf.Ensemble(cfgs) as ens:
+        tune = ens.autotune(10)
+        ens.step(10)
+        ms = ens.step_profiled(steps)
+        diverged = [b for b in range(len(cfgs)) if int(ens.reduce(b).nonfinite) > 0]
+    seq_ms = 0.0
+    for c in cfgs:
+        with pf.Simulation(c) as s:
+            s.step(10)
+            tot, _ = s.step_profiled(steps)
+            seq_ms += tot
+    return {"study": "ensemble", "boxes": len(cfgs), "nodes": total_nodes, "steps": steps, "autotune": tune,
+            "batched_mlups": round(total_nodes * steps / (ms / 1e3) / 1e6, 1),
+            "sequential_mlups": round(total_nodes * steps / (seq_ms / 1e3) / 1e6, 1),
+            "speedup": round(seq_ms / ms, 3), "diverged_boxes": diverged}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -324,7 +506,23 @@ def main():
     ap.add_argument("--workload", default="jet_d3q27")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--nz", type=int, default=0, help="override the workload's z extent (profiling captures)")
+    ap.add_argument("--study", choices=["precision", "closure", "ensemble"], help="run a study instead of the bench line")
+    ap.add_argument("--ensemble-steps", type=int, default=2000)
+    ap.add_argument("--snapshots", type=int, default=20)
+    ap.add_argument("--snapshot-every", type=int, default=500)
+    ap.add_argument("--sample-stride", type=int, default=2)
+    ap.add_argument("--train-iters", type=int, default=3000)
+    ap.add_argument("--train-batch", type=int, default=16384)
+    ap.add_argument("--train-lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--extra-strengths", type=float, nargs="*", default=[0.5, 2.0])
+    ap.add_argument("--checkpoints", default="500,1000,2000,5000,10000")
     args = ap.parse_args()
+    if args.study:
+        run = {"precision": run_precision_study, "closure": run_closure_study, "ensemble": run_ensemble_study}[args.study]
+        print(json.dumps(run(args)), flush=True)
+        return
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     ranks = Ranks()

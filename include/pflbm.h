@@ -269,6 +269,49 @@ int pflbm_ensemble_autotune(pflbm_ensemble *ens, int32_t trial_steps, int32_t *b
 int pflbm_ensemble_info(const pflbm_ensemble *ens, uint64_t *total_nodes, int32_t *n_boxes, int32_t *n_items);
 int pflbm_ensemble_destroy(pflbm_ensemble *ens);
 
+/* ---- learned eddy-viscosity closure (no counterpart in the reference) ---
+ * An MLP maps the per-node features (Pi_xx, Pi_yy, Pi_zz, Pi_xy, Pi_xz,
+ * Pi_yz, phi, |grad phi|) to an eddy viscosity nu_t >= 0 that the collision
+ * adds to the relaxation time (tau += 3 * strength * nu_t; the reference's
+ * constant-tau collision, lbm.cu:158-170, is strength 0 / no closure).
+ * Network: 8 -> 32 -> 32 -> 1, SiLU hidden layers, softplus output.
+ * Blob (PFLBM_MLP_BLOB floats): W1[32][8], b1[32], W2[32][32], b2[32],
+ * w3[32], b3, feature mean[8], feature inv_scale[8], out_scale, strength.
+ *
+ * Training data are box-filtered (3x3x3) and 2x-restricted snapshots of a
+ * fine FP32 run of this solver: features as the coarse solver would carry
+ * them and the least-squares eddy viscosity of the sub-filter stress as the
+ * target. Forward, backward and Adam run as CUDA kernels. */
+#define PFLBM_MLP_PARAMS 1377
+#define PFLBM_MLP_BLOB 1395
+typedef struct pflbm_closure pflbm_closure;
+int pflbm_closure_create(int32_t device, uint64_t max_samples, pflbm_closure **out);
+/* Appends the samples of the fine simulation's current state (coarse nodes
+ * with x and y multiples of stride, all interior z). */
+int pflbm_closure_add_snapshot(pflbm_closure *c, pflbm_sim *fine, int32_t stride, uint64_t *added);
+int pflbm_closure_num_samples(const pflbm_closure *c, uint64_t *n);
+/* Samples as host arrays x[n][8], y[n]; set_samples replaces the data set. */
+int pflbm_closure_get_samples(pflbm_closure *c, uint64_t first, uint64_t count, float *host_x, float *host_y);
+int pflbm_closure_set_samples(pflbm_closure *c, const float *host_x, const float *host_y, uint64_t count);
+/* Feature normalisation and out_scale from the data, Glorot-uniform weights
+ * from a counter hash of seed; resets Adam. */
+int pflbm_closure_init_params(pflbm_closure *c, uint32_t seed);
+int pflbm_closure_get_blob(pflbm_closure *c, float *host_blob);
+int pflbm_closure_set_blob(pflbm_closure *c, const float *host_blob);
+/* Summed gradient of the loss (softplus(z) - y/out_scale)^2 over the first
+ * count samples, FP64 accumulation of FP32 per-block sums. */
+int pflbm_closure_gradient(pflbm_closure *c, uint64_t count, double *host_grad, double *loss_sum);
+/* Adam (beta 0.9/0.999, eps 1e-8) on minibatches drawn by a counter hash;
+ * loss_history (may be NULL) receives the mean minibatch loss per iteration. */
+int pflbm_closure_train(pflbm_closure *c, int32_t iterations, int32_t batch, float lr, uint32_t seed,
+                        double *loss_history);
+int pflbm_closure_loss(pflbm_closure *c, double *mean_loss);
+int pflbm_closure_destroy(pflbm_closure *c);
+/* Attaches a trained network to a simulation (FP32 or FP64 storage; NULL
+ * detaches): the weights are rounded to BF16 and run in the collide kernel,
+ * the result scaled by strength (>= 0). */
+int pflbm_set_closure(pflbm_sim *sim, const float *blob, float strength);
+
 #ifdef __cplusplus
 }
 #endif

@@ -178,6 +178,19 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
                                     ctypes.c_int),
         "pflbm_ensemble_info": ([vp, ctypes.POINTER(u64), ctypes.POINTER(i32), ctypes.POINTER(i32)], ctypes.c_int),
         "pflbm_ensemble_destroy": ([vp], ctypes.c_int),
+        "pflbm_closure_create": ([i32, u64, ctypes.POINTER(vp)], ctypes.c_int),
+        "pflbm_closure_add_snapshot": ([vp, vp, i32, ctypes.POINTER(u64)], ctypes.c_int),
+        "pflbm_closure_num_samples": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
+        "pflbm_closure_get_samples": ([vp, u64, u64, vp, vp], ctypes.c_int),
+        "pflbm_closure_set_samples": ([vp, vp, vp, u64], ctypes.c_int),
+        "pflbm_closure_init_params": ([vp, u32], ctypes.c_int),
+        "pflbm_closure_get_blob": ([vp, vp], ctypes.c_int),
+        "pflbm_closure_set_blob": ([vp, vp], ctypes.c_int),
+        "pflbm_closure_gradient": ([vp, u64, vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "pflbm_closure_train": ([vp, i32, i32, ctypes.c_float, u32, vp], ctypes.c_int),
+        "pflbm_closure_loss": ([vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "pflbm_closure_destroy": ([vp], ctypes.c_int),
+        "pflbm_set_closure": ([vp, vp, ctypes.c_float], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -219,6 +232,7 @@ def preset(name: str, **overrides) -> Config:
     jet_d3q19        the same jet in D3Q19
     jet_precision    D3Q19 256x256x1024, D=32
     jet_closure      D3Q19 128x128x512, D=16, Re=10000
+    jet_closure_fine the same jet on the 2x finer grid: 256x256x1024, D=32
     """
     lib = load_library()
     c = Config()
@@ -228,15 +242,15 @@ def preset(name: str, **overrides) -> Config:
         c.radius, c.diam = 16, 32
         c.tau, c.sigma, c.gamma = 0.6, 0.01, 0.05
         c.droplet_x_stretch = 1.0
-    elif name in ("jet_d3q27", "jet_d3q19", "jet_precision", "jet_closure"):
+    elif name in ("jet_d3q27", "jet_d3q19", "jet_precision", "jet_closure", "jet_closure_fine"):
         vs = VS_D3Q27 if name == "jet_d3q27" else VS_D3Q19
         _check(lib, lib.pflbm_config_reference(ctypes.byref(c), CASE_JET, vs))
-        if name == "jet_precision":
+        if name in ("jet_precision", "jet_closure_fine"):
             c.nx, c.ny, c.nz, c.diam = 256, 256, 1024, 32
         else:
             c.nx, c.ny, c.nz, c.diam = 128, 128, 512, 16
         c.radius = c.diam // 2
-        re = 10000.0 if name == "jet_closure" else 5000.0
+        re = 10000.0 if name.startswith("jet_closure") else 5000.0
         c.reynolds_water = c.reynolds_oil = re
         c.u_inf = 0.05
         # sigma = u^2 D / We with We = 500, computed in float as constants.cuh:98
@@ -463,3 +477,106 @@ class Simulation:
         v = ctypes.c_int32()
         _check(self.lib, self.lib.pflbm_kernels_per_step(self._h, ctypes.byref(v)))
         return int(v.value)
+
+    def set_closure(self, blob, strength: float = 1.0):
+        """Attaches a closure network (PFLBM_MLP_BLOB floats; None detaches)."""
+        if blob is None:
+            _check(self.lib, self.lib.pflbm_set_closure(self._h, None, 0.0))
+            return
+        b = np.ascontiguousarray(blob, np.float32)
+        if b.size != MLP_BLOB:
+            raise ValueError(f"closure blob must hold {MLP_BLOB} floats")
+        _check(self.lib, self.lib.pflbm_set_closure(self._h, b.ctypes.data, float(strength)))
+
+
+MLP_PARAMS, MLP_BLOB = 1377, 1395
+
+
+def bf16_round(a: np.ndarray) -> np.ndarray:
+    """Round float32 values to BF16 precision (nearest even), as float32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    finite = (u & 0x7F800000) != 0x7F800000
+    r = np.where(finite, (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000, u & 0xFFFF0000)
+    return r.astype(np.uint32).view(np.float32)
+
+
+class Closure:
+    """Learned eddy-viscosity closure: training data, forward/backward/Adam
+    on the GPU (pflbm_closure_* in include/pflbm.h)."""
+
+    def __init__(self, max_samples: int, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.pflbm_closure_create(int(device), int(max_samples), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.pflbm_closure_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_snapshot(self, fine: "Simulation", stride: int = 2) -> int:
+        n = ctypes.c_uint64()
+        _check(self.lib, self.lib.pflbm_closure_add_snapshot(self._h, fine._h, int(stride), ctypes.byref(n)))
+        return int(n.value)
+
+    @property
+    def num_samples(self) -> int:
+        n = ctypes.c_uint64()
+        _check(self.lib, self.lib.pflbm_closure_num_samples(self._h, ctypes.byref(n)))
+        return int(n.value)
+
+    def samples(self, first: int = 0, count: int | None = None):
+        count = self.num_samples - first if count is None else count
+        x = np.empty((count, 8), np.float32)
+        y = np.empty(count, np.float32)
+        _check(self.lib, self.lib.pflbm_closure_get_samples(self._h, first, count, x.ctypes.data, y.ctypes.data))
+        return x, y
+
+    def set_samples(self, x: np.ndarray, y: np.ndarray):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        _check(self.lib, self.lib.pflbm_closure_set_samples(self._h, x.ctypes.data, y.ctypes.data, len(y)))
+
+    def init_params(self, seed: int = 1):
+        _check(self.lib, self.lib.pflbm_closure_init_params(self._h, int(seed)))
+
+    @property
+    def blob(self) -> np.ndarray:
+        b = np.empty(MLP_BLOB, np.float32)
+        _check(self.lib, self.lib.pflbm_closure_get_blob(self._h, b.ctypes.data))
+        return b
+
+    @blob.setter
+    def blob(self, b):
+        b = np.ascontiguousarray(b, np.float32)
+        _check(self.lib, self.lib.pflbm_closure_set_blob(self._h, b.ctypes.data))
+
+    def gradient(self, count: int):
+        g = np.empty(MLP_PARAMS, np.float64)
+        loss = ctypes.c_double()
+        _check(self.lib, self.lib.pflbm_closure_gradient(self._h, int(count), g.ctypes.data, ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def train(self, iterations: int, batch: int = 8192, lr: float = 1e-3, seed: int = 7) -> np.ndarray:
+        hist = np.empty(iterations, np.float64)
+        _check(self.lib, self.lib.pflbm_closure_train(self._h, int(iterations), int(batch), float(lr), int(seed),
+                                                      hist.ctypes.data))
+        return hist
+
+    def loss(self) -> float:
+        v = ctypes.c_double()
+        _check(self.lib, self.lib.pflbm_closure_loss(self._h, ctypes.byref(v)))
+        return float(v.value)

@@ -21,7 +21,7 @@ DRIVER = BUILD / "pflbm_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
-SOURCES = ["api.cu", "engine_fp32.cu", "engine_fp64.cu", "engine_fp16.cu", "engine_bf16.cu", "ensemble.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "engine_fp32.cu", "engine_fp64.cu", "engine_fp16.cu", "engine_bf16.cu", "ensemble.cu", "noalloc.cu", "closure.cu"]
 HOST_SOURCES = ["driver_main.cpp"]
 
 

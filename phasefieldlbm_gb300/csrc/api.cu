@@ -326,6 +326,27 @@ std::string step6(uint64_t t) {
 
 }  // namespace
 
+namespace pflbm {
+int sim_view(pflbm_sim *s, SimView &v) {
+    if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
+    if (!s->initialized) return fail(PFLBM_ERR_STATE, "pflbm_init has not been called");
+    cudaSetDevice(s->device);
+    flush_initial(s);
+    int rc = ensure_cache(s);
+    if (rc) return rc;
+    v.macro = s->eng->macro_ptr();
+    v.real_bytes = s->eng->real_bytes();
+    v.nx = s->hp.nx;
+    v.ny = s->hp.ny;
+    v.nz = s->hp.nz;
+    v.N = s->hp.N;
+    v.device = s->device;
+    v.tau_water = s->hp.tau_water;
+    v.tau_oil = s->hp.tau_oil;
+    return PFLBM_OK;
+}
+}  // namespace pflbm
+
 extern "C" {
 
 int pflbm_abi_version(void) { return PFLBM_ABI_VERSION; }
@@ -583,6 +604,41 @@ int pflbm_reduce(pflbm_sim *s, pflbm_diag *d) {
     if (d->nonfinite > 0) return fail(PFLBM_ERR_DIVERGED, "non-finite values in rho, u or phi");
     return PFLBM_OK;
 }
+
+int pflbm_set_closure(pflbm_sim *s, const float *blob, float strength) {
+    if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
+    if (blob && !(strength >= 0.0f)) return fail(PFLBM_ERR_INVALID_ARG, "strength must be >= 0");
+    cudaSetDevice(s->device);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    std::vector<float> w;
+    if (blob) {
+        // the network runs with BF16 weights (round to nearest even); the
+        // normalisation constants, out_scale and strength stay FP32
+        w.assign(blob, blob + pflbm::kMlpBlobFloats);
+        for (int i = 0; i < pflbm::kMlpParamFloats; ++i) {
+            uint32_t u;
+            std::memcpy(&u, &w[i], 4);
+            if ((u & 0x7f800000u) != 0x7f800000u) u += 0x7fffu + ((u >> 16) & 1u);
+            u &= 0xffff0000u;
+            std::memcpy(&w[i], &u, 4);
+        }
+        w[pflbm::kMlpBlobFloats - 1] = strength;
+    }
+    std::string err;
+    int rc = s->eng->set_closure(blob ? w.data() : nullptr, err);
+    if (rc) return fail(rc, err);
+    // steps are captured with the collide kernel of the current mode
+    destroy_graphs(s);
+    const int counts[3] = {1, 2, kChunk};
+    for (int par = 0; par < 2; ++par)
+        for (int k = 0; k < 3; ++k) {
+            rc = capture(s, par, counts[k], &s->graphs[par][k]);
+            if (rc) return rc;
+        }
+    return PFLBM_OK;
+}
+
 
 int pflbm_write_output(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
     if (!s || !dir || (!ids && n > 0) || n < 0) return fail(PFLBM_ERR_INVALID_ARG, "bad argument");

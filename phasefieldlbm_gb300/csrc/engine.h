@@ -69,7 +69,28 @@ class Engine {
     // True when the TMA-fed collide kernel is in use.
     virtual bool uses_tma() const = 0;
     virtual int kernels_per_step() const = 0;
+    // Learned closure: copies the network blob (kMlpBlob floats, host) to the
+    // device and switches the collide kernel to the closure mode; null
+    // detaches. PFLBM_ERR_UNSUPPORTED for 16-bit storage.
+    virtual int set_closure(const float *host_blob, std::string &err) = 0;
+    virtual bool has_closure() const = 0;
 };
+
+// Device view of a simulation's macroscopic fields (analysis cache brought
+// up to date and synchronised) for the closure's training-data kernels.
+// Closure network blob: kMlpParamFloats weights, then mean[8],
+// inv_scale[8], out_scale, strength (kernels.cuh kMlp* offsets).
+constexpr int kMlpParamFloats = 1377, kMlpBlobFloats = 1395;
+
+struct SimView {
+    const void *macro;  // 18*N reals, pflbm_field_id order
+    int real_bytes;
+    uint32_t nx, ny, nz;
+    uint64_t N;
+    int device;
+    double tau_water, tau_oil;
+};
+int sim_view(pflbm_sim *s, SimView &v);
 
 // api.cu: derived constants, validation and the thread-local error message.
 void derive(const pflbm_config &c, HostParams &h);

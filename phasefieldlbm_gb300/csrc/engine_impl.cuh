@@ -168,9 +168,11 @@ class EngineT final : public Engine {
     }
 
     void free_all() override {
-        void *ptrs[] = {f_[0], f_[1], phi_[0], phi_[1], j_, top_, macro_, counters_, partial_, avg_, vort_, err_};
+        void *ptrs[] = {f_[0], f_[1], phi_[0], phi_[1], j_, top_, macro_, counters_, partial_, avg_, vort_, err_, mlp_};
         for (void *q : ptrs)
             if (q) cudaFree(q);
+        mlp_ = nullptr;
+        closure_ = false;
         f_[0] = f_[1] = nullptr;
         phi_[0] = phi_[1] = nullptr;
         j_ = top_ = macro_ = avg_ = vort_ = nullptr;
@@ -194,6 +196,7 @@ class EngineT final : public Engine {
         b.avg = avg_;
         b.macro = macro_;
         b.err = err_;
+        b.mlp = mlp_;
         return b;
     }
 
@@ -208,7 +211,15 @@ class EngineT final : public Engine {
     void enqueue_step(int parity, cudaStream_t s, cudaEvent_t *ev) override {
         const StepBuffers<S, T> b = buffers(parity);
         if (ev) cudaEventRecord(ev[0], s);
-        if (use_tma_) {
+        if (closure_) {
+            // learned closure: plain-load kernel with the network in shared memory
+            if constexpr (sizeof(S) >= 4) {
+                if (avg_)
+                    k_collide<QQ, JET, S, MODE_STEP_CLOSURE_AVG><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
+                else
+                    k_collide<QQ, JET, S, MODE_STEP_CLOSURE><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
+            }
+        } else if (use_tma_) {
             const size_t sm = TmaLayout<QQ, S>::total;
             if (avg_)
                 k_collide_tma<QQ, JET, S, MODE_STEP_AVG>
@@ -225,7 +236,7 @@ class EngineT final : public Engine {
         if (ev) cudaEventRecord(ev[2], s);
         if constexpr (std::is_same<T, float>::value) {
             if (h_.nx % 4 == 0 && !no_vec_) {
-                const dim3 g4((h_.nx / 4 + 31) / 32, (h_.ny + 7) / 8, h_.nz);
+                const dim3 g4((h_.nx / 4 + 31) / 32, (h_.ny + 7) / 8, JET ? h_.nz + 4 : h_.nz);
                 k_phase_v4<QQ, JET, S><<<g4, node_block(), 0, s>>>(p_, b);
             } else {
                 k_phase<QQ, JET, S><<<node_grid(), node_block(), 0, s>>>(p_, b);
@@ -293,6 +304,32 @@ class EngineT final : public Engine {
     void *vort_ptr() override { return vort_; }
     uint64_t device_bytes() const override { return bytes_; }
     int kernels_per_step() const override { return 2; }
+    int set_closure(const float *host_blob, std::string &err) override {
+        if constexpr (sizeof(S) < 4) {
+            err = "the learned closure needs FP32 or FP64 storage";
+            return PFLBM_ERR_UNSUPPORTED;
+        } else {
+            if (!host_blob) {
+                closure_ = false;
+                return PFLBM_OK;
+            }
+            if (!mlp_) {
+                if (cudaMalloc(&mlp_, sizeof(float) * kMlpBlob) != cudaSuccess) {
+                    cudaGetLastError();
+                    err = "cudaMalloc failed (closure network)";
+                    return PFLBM_ERR_OUT_OF_MEMORY;
+                }
+                bytes_ += sizeof(float) * kMlpBlob;
+            }
+            if (cudaMemcpy(mlp_, host_blob, sizeof(float) * kMlpBlob, cudaMemcpyHostToDevice) != cudaSuccess) {
+                err = cudaGetErrorString(cudaGetLastError());
+                return PFLBM_ERR_CUDA;
+            }
+            closure_ = true;
+            return PFLBM_OK;
+        }
+    }
+    bool has_closure() const override { return closure_; }
 
    private:
     static constexpr int kRedBlocks = 608;
@@ -307,6 +344,8 @@ class EngineT final : public Engine {
     unsigned int *err_ = nullptr;
     bool use_tma_ = false;
     bool no_vec_ = false;  // PFLBM_NO_VEC=1: scalar phase kernel
+    float *mlp_ = nullptr;  // closure network blob (kMlpBlob floats)
+    bool closure_ = false;
     CUtensorMap fmap_[2]{}, phimap_[2]{};
     uint64_t bytes_ = 0;
 };

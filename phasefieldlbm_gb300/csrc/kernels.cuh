@@ -35,6 +35,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "lattice.cuh"
 #include "params.cuh"
 #include "tile.h"
@@ -45,7 +47,9 @@ constexpr int TX = PFLBM_TILE_X, TY = PFLBM_TILE_Y, NT = TX * TY;
 constexpr int PX = TX + 4, PY = TY + 4;  // phi tile + halo 2
 constexpr int NX_ = TX + 2, NY_ = TY + 2;  // normal tile + halo 1
 
-enum Mode { MODE_STEP = 0, MODE_STEP_AVG = 1, MODE_ANALYSIS = 2, MODE_STEP_CLOSURE = 3 };
+enum Mode { MODE_STEP = 0, MODE_STEP_AVG = 1, MODE_ANALYSIS = 2, MODE_STEP_CLOSURE = 3, MODE_STEP_CLOSURE_AVG = 4 };
+constexpr bool mode_closure(int m) { return m == MODE_STEP_CLOSURE || m == MODE_STEP_CLOSURE_AVG; }
+constexpr bool mode_average(int m) { return m == MODE_STEP_AVG || m == MODE_STEP_CLOSURE_AVG; }
 
 // ------------------------------------------------------------ closure MLP
 // Eddy-viscosity network of the learned closure: x = (Pi_xx, Pi_yy, Pi_zz,
@@ -159,27 +163,50 @@ __device__ __forceinline__ T sponge_ramp(const Params<T> &p, int z) {
 // Lattice-weighted central gradient of src/phaseField.cuh:67-118: pairs
 // (2k-1, 2k) in ascending k, (+c member) - (-c member), accumulated per
 // weight class, then w1*S1 + w2*S2 (+ w3*S3).
-template <int QQ, class T, class Get>
-__device__ __forceinline__ T lattice_grad(const Get &v, const int *ca) {
-    T s[3] = {T(0), T(0), T(0)};
-    bool first[3] = {true, true, true};
-#pragma unroll
-    for (int q = 1; q < QQ; q += 2) {
-        if (ca[q] != 0) {
-            const int cls = q <= 6 ? 0 : (q <= 18 ? 1 : 2);
-            const int qp = ca[q] > 0 ? q : q + 1;
-            const int qm = ca[q] > 0 ? q + 1 : q;
-            const T a = v(kCX[qp], kCY[qp], kCZ[qp]);
-            const T b = v(kCX[qm], kCY[qm], kCZ[qm]);
-            if (first[cls]) {
-                s[cls] = a - b;
-                first[cls] = false;
-            } else {
-                s[cls] = s[cls] + a;
-                s[cls] = s[cls] - b;
-            }
+namespace detail {
+// Direction components as constant expressions (same table as kCX/kCY/kCZ),
+// so that every stencil offset below is resolved at compile time.
+__host__ __device__ constexpr int dir_c(int axis, int q) {
+    constexpr int cx[27] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1, -1, 1};
+    constexpr int cy[27] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1, 1, -1, 1, -1, -1, 1, 1, -1};
+    constexpr int cz[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1, 1, -1, -1, 1, 1, -1, 1, -1};
+    return axis == 0 ? cx[q] : (axis == 1 ? cy[q] : cz[q]);
+}
+
+template <int AXIS, int Q, class T, class Get>
+__device__ __forceinline__ void grad_pair(const Get &v, T (&s)[3], bool (&first)[3]) {
+    constexpr int c = dir_c(AXIS, Q);
+    if constexpr (c != 0) {
+        constexpr int cls = Q <= 6 ? 0 : (Q <= 18 ? 1 : 2);
+        constexpr int qp = c > 0 ? Q : Q + 1;
+        constexpr int qm = c > 0 ? Q + 1 : Q;
+        const T a = v(dir_c(0, qp), dir_c(1, qp), dir_c(2, qp));
+        const T b = v(dir_c(0, qm), dir_c(1, qm), dir_c(2, qm));
+        if (first[cls]) {
+            s[cls] = a - b;
+            first[cls] = false;
+        } else {
+            s[cls] = s[cls] + a;
+            s[cls] = s[cls] - b;
         }
     }
+}
+
+template <int AXIS, class T, class Get, int... K>
+__device__ __forceinline__ void grad_pairs(const Get &v, T (&s)[3], bool (&first)[3],
+                                           std::integer_sequence<int, K...>) {
+    (grad_pair<AXIS, 2 * K + 1>(v, s, first), ...);
+}
+}  // namespace detail
+
+// Lattice-weighted central gradient of src/phaseField.cuh:67-118: pairs
+// (2k-1, 2k) in ascending k, (+c member) - (-c member), accumulated per
+// weight class, then w1*S1 + w2*S2 (+ w3*S3). AXIS 0, 1, 2 = x, y, z.
+template <int QQ, int AXIS, class T, class Get>
+__device__ __forceinline__ T lattice_grad(const Get &v) {
+    T s[3] = {T(0), T(0), T(0)};
+    bool first[3] = {true, true, true};
+    detail::grad_pairs<AXIS>(v, s, first, std::make_integer_sequence<int, (QQ - 1) / 2>{});
     T r = static_cast<T>(Weights<QQ>::w1) * s[0] + static_cast<T>(Weights<QQ>::w2) * s[1];
     if constexpr (QQ == 27) r += static_cast<T>(Weights<QQ>::w3) * s[2];
     return r;
@@ -209,7 +236,7 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
 
     // learned eddy-viscosity increment, in units of tau (tau = 1/2 + 3 nu)
     T tau_t = T(0);
-    if constexpr (MODE == MODE_STEP_CLOSURE) {
+    if constexpr (mode_closure(MODE)) {
         const T feat[kMlpIn] = {m.pxx, m.pyy, m.pzz, m.pxy, m.pxz, m.pyz, phi, ind};
         tau_t = T(3) * (T(s_mlp[kMlpStrength]) * mlp_nu_t<T>(s_mlp, feat));
     }
@@ -318,7 +345,7 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
                 bp[8 * plane + c2] = m.pyz;
             }
         }
-        if constexpr (MODE == MODE_STEP_AVG) {
+        if constexpr (mode_average(MODE)) {
             // derived fields (timeAverage.cuh:57-60, reynoldsMoments.cuh:57-60)
             const T tf = static_cast<T>(t + 1u);
             T *av = b.avg;
@@ -405,9 +432,9 @@ __device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> 
                 auto v = [&](int dx, int dy, int dz) -> T {
                     return s_phi[dz < 0 ? sm : (dz > 0 ? sp : s0)][ly + 1 + dy][lx + 1 + dx];
                 };
-                const T gxv = T(3) * lattice_grad<QQ, T>(v, kCX);
-                const T gyv = T(3) * lattice_grad<QQ, T>(v, kCY);
-                const T gzv = T(3) * lattice_grad<QQ, T>(v, kCZ);
+                const T gxv = T(3) * lattice_grad<QQ, 0, T>(v);
+                const T gyv = T(3) * lattice_grad<QQ, 1, T>(v);
+                const T gzv = T(3) * lattice_grad<QQ, 2, T>(v);
                 ind = sqrt(gxv * gxv + gyv * gyv + gzv * gzv);
                 const T inv = T(1) / (ind + static_cast<T>(1e-9));
                 nxv = gxv * inv;
@@ -457,9 +484,9 @@ __device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> 
         auto nv = [&](int c, int dx, int dy, int dz) -> T {
             return s_n[c][dz < 0 ? s_m : (dz > 0 ? s_p : s_0)][ty + 1 + dy][tx + 1 + dx];
         };
-        const T scx = lattice_grad<QQ, T>([&](int dx, int dy, int dz) { return nv(0, dx, dy, dz); }, kCX);
-        const T scy = lattice_grad<QQ, T>([&](int dx, int dy, int dz) { return nv(1, dx, dy, dz); }, kCY);
-        const T scz = lattice_grad<QQ, T>([&](int dx, int dy, int dz) { return nv(2, dx, dy, dz); }, kCZ);
+        const T scx = lattice_grad<QQ, 0, T>([&](int dx, int dy, int dz) { return nv(0, dx, dy, dz); });
+        const T scy = lattice_grad<QQ, 1, T>([&](int dx, int dy, int dz) { return nv(1, dx, dy, dz); });
+        const T scz = lattice_grad<QQ, 2, T>([&](int dx, int dy, int dz) { return nv(2, dx, dy, dz); });
         const T curvature = T(3) * (scx + scy + scz);
         const T n_x = nv(0, 0, 0, 0), n_y = nv(1, 0, 0, 0), n_z = nv(2, 0, 0, 0), ind = nv(3, 0, 0, 0);
         const T phi = s_phi[z % 3][ty + 2][tx + 2];
@@ -471,8 +498,8 @@ template <int QQ, bool JET, class S, int MODE>
 __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : PFLBM_COLLIDE_MIN_BLOCKS))
     k_collide(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b) {
     __shared__ CollideSmem<typename Store<S>::T> sm;
-    __shared__ float s_mlp[MODE == MODE_STEP_CLOSURE ? kMlpBlob : 1];
-    if constexpr (MODE == MODE_STEP_CLOSURE) {
+    __shared__ float s_mlp[mode_closure(MODE) ? kMlpBlob : 1];
+    if constexpr (mode_closure(MODE)) {
         for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpBlob; i += NT) s_mlp[i] = b.mlp[i];
         __syncthreads();
     }
@@ -614,29 +641,43 @@ __global__ void __launch_bounds__(256) k_phase(const Params<typename Store<S>::T
     phase_node<QQ, JET, S>(p, b, x, y, z, t);
 }
 
+// Boundary-plane nodes of the jet, kept out of line so that their rebuild
+// code does not set the register budget of the vectorised interior path.
+template <int QQ, bool JET, class S>
+__device__ __noinline__ void phase_node_outlined(const Params<float> &p, const StepBuffers<S, float> &b, int x, int y,
+                                                 int z, uint32_t t) {
+    phase_node<QQ, JET, S>(p, b, x, y, z, t);
+}
+
 // FP32 phase step with 128-bit accesses: one thread owns 4 consecutive x
 // nodes (nx % 4 == 0), reads the phi/J rows of its y and z neighbours as
 // float4 and the two x-end neighbours (periodically wrapped) as scalars.
-// The jet's boundary planes z = 1 and nz-2 go through phase_node.
+// The jet's boundary planes z = 1 and nz-2 go through phase_node, one node
+// per thread, in grid slices of their own.
 template <int QQ, bool JET, class S>
-__global__ void __launch_bounds__(256) k_phase_v4(const Params<float> p, const StepBuffers<S, float> b) {
+__global__ void __launch_bounds__(256, 4)
+    k_phase_v4(const __grid_constant__ Params<float> p, const __grid_constant__ StepBuffers<S, float> b) {
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const uint64_t N = p.N, plane = p.plane;
+    const uint64_t N = p.N;
     const int x4 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
     const uint32_t t = static_cast<uint32_t>(*b.step_in);
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0 &&
-        threadIdx.z == 0)
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
         *b.step_out = *b.step_in + 1ull;
-    if (x4 >= nx || y < 1 || y > ny - 2 || z < 1 || z > nz - 2) return;
-    if (JET && (z == 1 || z == nz - 2)) {
-        for (int k = 0; k < 4; ++k) {
-            const int x = x4 + k;
-            if (x >= 1 && x <= nx - 2) phase_node<QQ, JET, S>(p, b, x, y, z, t);
+    int z = blockIdx.z;
+    if constexpr (JET) {
+        // grid.z = nz + 4: slices 0-3 and 4-7 are the boundary planes 1 and
+        // nz-2, one node per thread (x = x4 + slice), scheduled first because
+        // their rebuilds are the longest; slices 8.. are planes 2 .. nz-3
+        if (blockIdx.z < 8) {
+            const int zb = blockIdx.z < 4 ? 1 : nz - 2;
+            const int x = x4 + (blockIdx.z & 3);
+            if (x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2) phase_node_outlined<QQ, JET, S>(p, b, x, y, zb, t);
+            return;
         }
-        return;
+        z = blockIdx.z - 6;
     }
+    if (x4 >= nx || y < 1 || y > ny - 2 || z < 1 || z > nz - 2) return;
     const int ym = wrapi(y - 1, ny), yp = wrapi(y + 1, ny);
     const int zm = JET ? z - 1 : wrapi(z - 1, nz), zp = JET ? z + 1 : wrapi(z + 1, nz);
     auto row = [&](int yy, int zz) -> uint64_t { return static_cast<uint64_t>(nx) * (yy + static_cast<uint64_t>(ny) * zz); };

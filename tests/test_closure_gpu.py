@@ -1,0 +1,182 @@
+"""The learned closure: GPU forward/backward against the FP64 oracle, GPU
+training, the closure-coupled collision against the oracle's, and the
+training-data kernels against a NumPy restatement of the filter/restrict
+pipeline.
+
+Tolerances: gradients rel L2 <= 1e-4 (FP32 kernels vs FP64 oracle);
+closure-coupled FP64 run <= 1e-10 (same semantics rule as the plain FP64
+path); training-data features rel L2 <= 1e-5, targets <= 1e-3 (FP32 kernels
+vs FP64 NumPy; the target is a ratio of small differences), leaving out the
+few samples within 0.1% of the strain threshold or of the cap.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _features(n, seed):
+    r = np.random.default_rng(seed)
+    x = np.empty((n, 8))
+    x[:, :6] = r.normal(0.0, 1e-4, (n, 6))   # Pi components
+    x[:, 6] = r.uniform(0.0, 1.0, n)          # phi
+    x[:, 7] = r.exponential(0.05, n)          # |grad phi|
+    return x
+
+
+def _split(blob):
+    return blob[:1377], blob[1377:1385], blob[1385:1393], float(blob[1393])
+
+
+def test_gradient_matches_oracle(pflbm, oracle):
+    n = 300  # not a multiple of the 128-sample block
+    x = _features(n, 1)
+    y = np.abs(np.random.default_rng(2).normal(2e-4, 1e-4, n))
+    with pflbm.Closure(1000) as c:
+        c.set_samples(x, y)
+        c.init_params(seed=3)
+        blob = c.blob.copy()
+        # move off the initial point so every layer has non-trivial gradients
+        blob[:1377] += np.random.default_rng(4).normal(0.0, 0.05, 1377).astype(np.float32)
+        c.blob = blob
+        g, loss = c.gradient(n)
+    p, mu, sc, osc = _split(blob.astype(np.float64))
+    out, g_ref = oracle.mlp_eval(p, mu, sc, osc, x.astype(np.float32).astype(np.float64),
+                                 y.astype(np.float32).astype(np.float64), with_grad=True)
+    loss_ref = float(np.sum((out / osc - y.astype(np.float32) / osc) ** 2))
+    assert rel_l2(g, g_ref) <= 1e-4, rel_l2(g, g_ref)
+    for name, sl in (("W1", slice(0, 256)), ("W2", slice(288, 1312)), ("w3", slice(1344, 1376))):
+        assert rel_l2(g[sl], g_ref[sl]) <= 1e-4, name
+    assert loss == pytest.approx(loss_ref, rel=1e-4)
+
+
+def test_training_fits_a_known_closure(pflbm):
+    n = 200_000
+    x = _features(n, 5)
+    xs = (x - x.mean(0)) / x.std(0)
+    y = 3e-4 * np.log1p(np.exp(0.8 * xs[:, 0] - 0.6 * xs[:, 6] + 0.3 * xs[:, 7]))
+    with pflbm.Closure(n) as c:
+        c.set_samples(x, y)
+        c.init_params(seed=11)
+        l0 = c.loss()
+        hist = c.train(800, batch=4096, lr=3e-3, seed=5)
+        l1 = c.loss()
+    print("loss", l0, "->", l1, "minibatch", hist[0], hist[-1])
+    assert np.all(np.isfinite(hist))
+    assert l1 < l0 / 20
+
+
+def test_closure_collision_matches_oracle(pflbm, oracle):
+    cfg = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
+    cfg.nx, cfg.ny, cfg.nz, cfg.diam, cfg.radius = 24, 24, 36, 8, 4
+    cfg.storage = pflbm.STORAGE_FP64
+    # seeded uniform inflow noise: no libm-dependent Gaussian draws, so the
+    # FP64 run matches the oracle to the 1e-10 semantics bar
+    cfg.inflow_noise, cfg.noise_amp, cfg.seed = pflbm.NOISE_UNIFORM_UZ, 0.05, 12345
+    # a network with a visible effect: out_scale 2e-3 -> tau increments ~1e-2
+    with pflbm.Closure(4096) as c:
+        c.set_samples(_features(4096, 7), np.full(4096, 2e-3))
+        c.init_params(seed=9)
+        blob = c.blob.copy()
+    blob[:1377] += np.random.default_rng(8).normal(0.0, 0.1, 1377).astype(np.float32)
+    steps = 20
+    with pflbm.Simulation(cfg) as s:
+        s.set_closure(blob, strength=1.0)
+        s.step(steps)
+        lib = {f: s.get_field(f, dtype=np.float64) for f in ("rho", "ux", "uy", "uz", "phi")}
+    with pflbm.Simulation(cfg) as s:
+        s.step(steps)
+        plain = {f: s.get_field(f, dtype=np.float64) for f in ("rho", "uz")}
+    p, mu, sc, osc = _split(blob.astype(np.float64))
+    o = oracle.OracleSim(cfg, fp64=True)
+    o.set_closure(pflbm.bf16_round(blob[:1377]).astype(np.float64), mu, sc, osc, 1.0)
+    o.step(steps)
+    for f in lib:
+        assert rel_l2(lib[f], o.get_field(f)) <= 1e-10, f
+    # the closure is active
+    assert rel_l2(lib["uz"], plain["uz"]) > 1e-6
+
+
+def _numpy_samples(fields, tau_w, tau_o, stride):
+    """Box filter (3x3x3 around fine node 2X), restriction, strain rate,
+    sub-filter stress, targets and features, in FP64."""
+    rho, ux, uy, uz, phi = (fields[k].astype(np.float64) for k in ("rho", "ux", "uy", "uz", "phi"))
+    nzf, nyf, nxf = rho.shape
+    nxc, nyc, nzc = nxf // 2, nyf // 2, nzf // 2
+    zi, yi, xi = np.meshgrid(np.arange(nzc), np.arange(nyc), np.arange(nxc), indexing="ij")
+
+    def filt(a):
+        acc = np.zeros((nzc, nyc, nxc))
+        for dz in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    Z = np.clip(2 * zi + dz, 0, nzf - 1)
+                    Y = np.clip(2 * yi + dy, 0, nyf - 1)
+                    X = np.clip(2 * xi + dx, 0, nxf - 1)
+                    acc += a[Z, Y, X]
+        return acc / 27.0
+
+    r, u, v, w, ph = filt(rho), filt(ux), filt(uy), filt(uz), filt(phi)
+    t = {"xx": filt(ux * ux) - u * u, "yy": filt(uy * uy) - v * v, "zz": filt(uz * uz) - w * w,
+         "xy": filt(ux * uy) - u * v, "xz": filt(ux * uz) - u * w, "yz": filt(uy * uz) - v * w}
+    i0 = ((2 + stride - 1) // stride) * stride
+    xs = np.arange(i0, nxc - 2, stride)
+    ys = np.arange(i0, nyc - 2, stride)
+    zs = np.arange(2, nzc - 2)
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+
+    def d(a, ax):
+        off = [0, 0, 0]
+        off[ax] = 1
+        return 0.5 * (a[Z + off[0], Y + off[1], X + off[2]] - a[Z - off[0], Y - off[1], X - off[2]])
+
+    vel = [u, v, w]
+    axis = {0: 2, 1: 1, 2: 0}  # x -> array axis 2
+    g = [[d(vel[b], axis[a]) for b in range(3)] for a in range(3)]
+    sxx, syy, szz = g[0][0], g[1][1], g[2][2]
+    sxy, sxz, syz = 0.5 * (g[0][1] + g[1][0]), 0.5 * (g[0][2] + g[2][0]), 0.5 * (g[1][2] + g[2][1])
+    tr = (sxx + syy + szz) / 3.0
+    rr, pp = r[Z, Y, X], ph[Z, Y, X]
+    c = -2.0 * rr * ((1 - pp) * tau_w + pp * tau_o) / 3.0
+    # D3Q19 lattice gradient of phi
+    dirs = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+    dirs2 = [(a, b, 0) for a in (1, -1) for b in (1, -1)] + [(a, 0, b) for a in (1, -1) for b in (1, -1)] + \
+            [(0, a, b) for a in (1, -1) for b in (1, -1)]
+    gx = gy = gz = 0.0
+    for (cx, cy, cz), wq in [(dd, 1 / 18) for dd in dirs] + [(dd, 1 / 36) for dd in dirs2]:
+        val = wq * ph[Z + cz, Y + cy, X + cx]
+        gx, gy, gz = gx + val * cx, gy + val * cy, gz + val * cz
+    ind = 3.0 * np.sqrt(gx * gx + gy * gy + gz * gz)
+    T = {k: a[Z, Y, X] for k, a in t.items()}
+    ttr = (T["xx"] + T["yy"] + T["zz"]) / 3.0
+    num = -((T["xx"] - ttr) * sxx + (T["yy"] - ttr) * syy + (T["zz"] - ttr) * szz
+            + 2 * (T["xy"] * sxy + T["xz"] * sxz + T["yz"] * syz))
+    den = 2 * (sxx ** 2 + syy ** 2 + szz ** 2 + 2 * (sxy ** 2 + sxz ** 2 + syz ** 2))
+    raw = np.maximum(0.0, num / np.where(den > 0, den, 1.0))
+    nu = np.where(den > 2e-10, np.minimum(raw, 2e-3), 0.0)
+    # samples whose classification (strain threshold, cap) FP32 rounding can flip
+    edge = (np.abs(den / 2e-10 - 1.0) < 1e-3) | (np.abs(raw / 2e-3 - 1.0) < 1e-3)
+    feats = np.stack([c * (sxx - tr), c * (syy - tr), c * (szz - tr), c * sxy, c * sxz, c * syz, pp, ind], -1)
+    return feats.reshape(-1, 8), nu.reshape(-1), edge.reshape(-1)
+
+
+def test_snapshot_samples_match_numpy(pflbm, oracle):
+    cfg = pflbm.preset("jet_closure")
+    cfg.nx, cfg.ny, cfg.nz, cfg.diam, cfg.radius = 48, 48, 96, 12, 6
+    stride = 2
+    with pflbm.Simulation(cfg) as s:
+        s.step(80)
+        fields = {f: s.get_field(f) for f in ("rho", "ux", "uy", "uz", "phi")}
+        tw, to = oracle.relaxation(cfg)[1:3]
+        with pflbm.Closure(200_000) as c:
+            added = c.add_snapshot(s, stride=stride)
+            x, y = c.samples()
+    xr, yr, edge = _numpy_samples(fields, tw, to, stride)
+    assert added == len(yr) == len(y)
+    for k in range(8):
+        assert rel_l2(x[:, k], xr[:, k]) <= 1e-5, k
+    assert edge.mean() < 0.01
+    assert rel_l2(y[~edge], yr[~edge]) <= 1e-3
+    assert np.count_nonzero(yr) > 0
