@@ -188,7 +188,11 @@ def workload_config(args):
     """The bench workload; --nz shortens the jet for profiling captures."""
     import phasefieldlbm_gb300 as pf
 
-    return pf.preset(args.workload, nz=args.nz) if args.nz else pf.preset(args.workload)
+    st = {"fp32": pf.STORAGE_FP32, "fp16": pf.STORAGE_FP16, "bf16": pf.STORAGE_BF16, "fp64": pf.STORAGE_FP64}
+    kw = {"storage": st[args.storage]}
+    if args.nz:
+        kw["nz"] = args.nz
+    return pf.preset(args.workload, **kw)
 
 
 def run_gpu(args, ranks: Ranks) -> dict:
@@ -199,7 +203,9 @@ def run_gpu(args, ranks: Ranks) -> dict:
     N = cfg.nodes
     q = int(cfg.velocity_set)
     s_f = {pf.STORAGE_FP32: 4, pf.STORAGE_FP64: 8, pf.STORAGE_FP16: 2, pf.STORAGE_BF16: 2}[int(cfg.storage)]
-    ba = b_alg(q, s_f, 4 if s_f != 8 else 8)
+    # canonical bytes per lattice update: g counted at the storage width of f
+    # for 16-bit runs (FP16/BF16 f and g, 112 B/LU for D3Q19), FP32 otherwise
+    ba = b_alg(q, s_f, s_f if s_f in (2, 8) else 4)
     sim = pf.Simulation(cfg)
     inner = args.inner
     # warm-up
@@ -301,9 +307,9 @@ def run_gpu(args, ranks: Ranks) -> dict:
     return {
         "metric": "MLUPS", "value": round(value, 2), "unit": "MLUPS", "n_gpus": ranks.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3 / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if s_f == 4 else str(s_f),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp16": "f16-storage/f32-math", "bf16": "bf16-storage/f32-math", "fp64": "f64"}[args.storage],
         "data": "synthetic",
-        "config": {"workload": f"jet D3Q{q}+D3Q7 FP32 {cfg.nx}x{cfg.ny}x{cfg.nz}, D={cfg.diam}, Re=5000, We=500, "
+        "config": {"workload": f"jet D3Q{q}+D3Q7 {args.storage.upper()} {cfg.nx}x{cfg.ny}x{cfg.nz}, D={cfg.diam}, Re=5000, We=500, "
                                "gamma=0.05, uniform 5% inflow noise (seed 12345)",
                    "preset": args.workload, "nodes": N, "lattice_steps_per_step": inner,
                    "l2": "inputs larger than L2 (f ping-pong 2x{:.0f} MB)".format(q * s_f * N / 1e6),
@@ -416,10 +422,19 @@ def run_closure_study(args) -> dict:
     n_snap, every = args.snapshots, args.snapshot_every
     fine_steps = n_snap * every
     coarse_steps = fine_steps // 2
-    fine_cfg = pf.preset("jet_closure_fine", flags=pf.FLAG_TIME_AVERAGE)
+    fx, fy, fz, fd = (int(v) for v in args.fine_grid.split(","))
+    fine_cfg = pf.preset("jet_closure_fine", flags=pf.FLAG_TIME_AVERAGE, nx=fx, ny=fy, nz=fz, diam=fd, radius=fd // 2)
+    fd2 = fd // 2
+    coarse_cfg = pf.preset("jet_closure", flags=pf.FLAG_TIME_AVERAGE, nx=fx // 2, ny=fy // 2, nz=fz // 2, diam=fd2,
+                           radius=fd2 // 2)
+    # sigma = u^2 D / We (We = 500) on each grid, as the presets compute it
+    for c in (fine_cfg, coarse_cfg):
+        c.sigma = float(np.float32(np.float32(np.float32(c.u_inf) * np.float32(c.u_inf)) * np.float32(c.diam)) /
+                        np.float32(500.0))
     stride = args.sample_stride
     per_snap = ((fine_cfg.nx // 2 - 3) // stride + 1) * ((fine_cfg.ny // 2 - 3) // stride + 1) * (fine_cfg.nz // 2 - 4)
-    out = {"study": "closure", "fine": "256x256x1024 D=32 Re=10000", "coarse": "128x128x512 D=16 Re=10000",
+    out = {"study": "closure", "fine": f"{fx}x{fy}x{fz} D={fd} Re=10000",
+           "coarse": f"{fx // 2}x{fy // 2}x{fz // 2} D={fd2} Re=10000",
            "fine_steps": fine_steps, "coarse_steps": coarse_steps, "snapshots": n_snap, "sample_stride": stride}
     with pf.Closure(per_snap * n_snap) as cl:
         with pf.Simulation(fine_cfg) as fine:
@@ -439,7 +454,7 @@ def run_closure_study(args) -> dict:
         blob = cl.blob
 
     def coarse_run(strength):
-        c = pf.preset("jet_closure", flags=pf.FLAG_TIME_AVERAGE)
+        c = coarse_cfg
         with pf.Simulation(c) as s:
             if strength > 0:
                 s.set_closure(blob, strength)
@@ -507,8 +522,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--nz", type=int, default=0, help="override the workload's z extent (profiling captures)")
+    ap.add_argument("--storage", choices=["fp32", "fp16", "bf16", "fp64"], default="fp32",
+                    help="population storage of the workload")
     ap.add_argument("--study", choices=["precision", "closure", "ensemble"], help="run a study instead of the bench line")
     ap.add_argument("--ensemble-steps", type=int, default=2000)
+    ap.add_argument("--fine-grid", default="256,256,1024,32", help="closure study: fine nx,ny,nz,D")
     ap.add_argument("--snapshots", type=int, default=20)
     ap.add_argument("--snapshot-every", type=int, default=500)
     ap.add_argument("--sample-stride", type=int, default=2)
