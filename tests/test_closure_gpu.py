@@ -180,3 +180,100 @@ def test_snapshot_samples_match_numpy(pflbm, oracle):
     assert edge.mean() < 0.01
     assert rel_l2(y[~edge], yr[~edge]) <= 1e-3
     assert np.count_nonzero(yr) > 0
+
+
+def test_tensor_core_network_matches_oracle(pflbm, oracle):
+    """FP32 runs evaluate the network with BF16 mma on the tensor cores (BF16
+    features and activations, FP32 accumulation): the change the closure
+    makes to the flow must match the FP64 oracle's change to within the BF16
+    activation rounding (5% on u_z)."""
+    cfg = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
+    cfg.nx, cfg.ny, cfg.nz, cfg.diam, cfg.radius = 40, 36, 48, 10, 5  # partial warps at the x edge
+    cfg.inflow_noise, cfg.noise_amp, cfg.seed = pflbm.NOISE_UNIFORM_UZ, 0.05, 12345
+    with pflbm.Closure(4096) as c:
+        c.set_samples(_features(4096, 7), np.full(4096, 2e-3))
+        c.init_params(seed=9)
+        blob = c.blob.copy()
+    blob[:1377] += np.random.default_rng(8).normal(0.0, 0.1, 1377).astype(np.float32)
+    steps = 20
+    res = {}
+    for strength in (0.0, 1.0):
+        with pflbm.Simulation(cfg) as s:
+            if strength:
+                s.set_closure(blob, strength=strength)
+            s.step(steps)
+            res[strength] = {f: s.get_field(f, dtype=np.float64) for f in ("rho", "uz", "phi")}
+    p, mu, sc, osc = _split(blob.astype(np.float64))
+    ora = {}
+    for strength in (0.0, 1.0):
+        o = oracle.OracleSim(cfg, fp64=True)
+        if strength:
+            o.set_closure(pflbm.bf16_round(blob[:1377]).astype(np.float64), mu, sc, osc, strength)
+        o.step(steps)
+        ora[strength] = {f: o.get_field(f) for f in ("rho", "uz", "phi")}
+    # u_z carries the closure's effect directly; phi only through advection,
+    # so its change is small and closer to the FP32 floor
+    for f, tol in (("uz", 5e-2), ("phi", 2e-1)):
+        d_lib = res[1.0][f] - res[0.0][f]
+        d_ora = ora[1.0][f] - ora[0.0][f]
+        print(f, "closure effect", np.linalg.norm(d_ora) / np.linalg.norm(ora[0.0][f]), "mismatch", rel_l2(d_lib, d_ora))
+        assert np.linalg.norm(d_ora) > 0
+        assert rel_l2(d_lib, d_ora) <= tol, (f, rel_l2(d_lib, d_ora))
+
+
+def _restrict_filtered(a):
+    nz, ny, nx = a.shape
+    acc = np.zeros((nz // 2, ny // 2, nx // 2))
+    for dz in (-1, 0, 1):
+        zi = np.clip(np.arange(nz // 2) * 2 + dz, 0, nz - 1)
+        for dy in (-1, 0, 1):
+            yi = np.clip(np.arange(ny // 2) * 2 + dy, 0, ny - 1)
+            for dx in (-1, 0, 1):
+                xi = np.clip(np.arange(nx // 2) * 2 + dx, 0, nx - 1)
+                acc += a[np.ix_(zi, yi, xi)]
+    return acc / 27.0
+
+
+def _jet_closure_pair(pflbm, nx, nz, diam):
+    def sig(c):
+        c.sigma = float(np.float32(np.float32(np.float32(c.u_inf) * np.float32(c.u_inf)) * np.float32(c.diam))
+                        / np.float32(500.0))
+        return c
+
+    fine = sig(pflbm.preset("jet_closure_fine", nx=nx, ny=nx, nz=nz, diam=diam, radius=diam // 2,
+                            flags=pflbm.FLAG_TIME_AVERAGE))
+    coarse = sig(pflbm.preset("jet_closure", nx=nx // 2, ny=nx // 2, nz=nz // 2, diam=diam // 2,
+                              radius=diam // 4, flags=pflbm.FLAG_TIME_AVERAGE))
+    return fine, coarse
+
+
+def test_trained_closure_beats_constant_tau(pflbm):
+    """The learned part end to end at a small scale: snapshots of a 2x-finer
+    run of the same seeded jet (Re = 10000), GPU training, then coarse runs
+    with and without the closure judged by the relative L2 error of their
+    time-averaged u_z and phi against the filtered fine average."""
+    fine_cfg, coarse_cfg = _jet_closure_pair(pflbm, 96, 384, 12)
+    snaps, every = 10, 200
+    with pflbm.Closure(2_000_000) as cl:
+        with pflbm.Simulation(fine_cfg) as fine:
+            for _ in range(snaps):
+                fine.step(every)
+                cl.add_snapshot(fine, stride=2)
+            ref = {f: _restrict_filtered(fine.get_field(f).astype(np.float64)) for f in ("avg_uz", "avg_phi")}
+        cl.init_params(seed=2026)
+        l0 = cl.loss()
+        cl.train(1000, batch=16384, lr=2e-3, seed=2026)
+        l1 = cl.loss()
+        blob = cl.blob
+    assert l1 < l0
+    err = {}
+    for name, strength in (("plain", 0.0), ("closure", 1.0)):
+        with pflbm.Simulation(coarse_cfg) as s:
+            if strength:
+                s.set_closure(blob, strength)
+            s.step(snaps * every // 2)
+            sl = (slice(2, -2),) * 3
+            err[name] = {f: rel_l2(s.get_field(f).astype(np.float64)[sl], ref[f][sl]) for f in ("avg_uz", "avg_phi")}
+    print("training loss", l0, "->", l1, "errors", err)
+    assert err["closure"]["avg_uz"] < err["plain"]["avg_uz"]
+    assert err["closure"]["avg_phi"] < 1.01 * err["plain"]["avg_phi"]
