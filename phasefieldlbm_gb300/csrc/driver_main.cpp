@@ -17,7 +17,7 @@
 //   --storage fp32|fp16|bf16|fp64
 //   --fields a,b,c  fields written at output steps (default rho,uz as main.cu:130-133)
 //   --average / --reynolds / --vorticity   derived fields (compile.sh:71-73)
-//   --nx/--ny/--nz/--diam/--radius/--sigma/--tau/--gamma/--reynolds/--u-inf  mesh and physics
+//   --nx/--ny/--nz/--diam/--radius/--sigma/--tau/--gamma/--re/--u-inf  mesh and physics
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -123,7 +123,7 @@ int main(int argc, char **argv) {
         else if (a == "--tau") cfg.tau = float(std::atof(next()));
         else if (a == "--gamma") cfg.gamma = float(std::atof(next()));
         else if (a == "--u-inf") cfg.u_inf = float(std::atof(next()));
-        else if (a == "--reynolds") cfg.reynolds_water = cfg.reynolds_oil = float(std::atof(next()));
+        else if (a == "--re") cfg.reynolds_water = cfg.reynolds_oil = float(std::atof(next()));
     }
     if (save <= 0) save = 1;
 

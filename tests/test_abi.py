@@ -81,3 +81,37 @@ def test_presets_are_valid_configs(pflbm):
     j = pflbm.preset("jet_d3q27")
     assert (j.nx, j.ny, j.nz, j.velocity_set, j.diam) == (128, 128, 512, 27, 16)
     assert abs(j.sigma - 8e-5) < 1e-9
+
+
+def test_header_is_plain_c_and_links(tmp_path, pflbm):
+    """include/pflbm.h compiles as C99 and a C program links libpflbm and
+    calls it (no GPU needed: configuration defaults and validation only)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = Path(pflbm.load_library()._name)
+    src = tmp_path / "abi.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "pflbm.h"
+int main(void) {
+    pflbm_config c;
+    if (pflbm_abi_version() != PFLBM_ABI_VERSION) return 2;
+    if (pflbm_config_reference(&c, PFLBM_CASE_JET, PFLBM_VS_D3Q19) != PFLBM_OK) return 3;
+    c.nz = 8;  /* rejected before any device work */
+    pflbm_sim *s = 0;
+    if (pflbm_create(&c, &s) != PFLBM_ERR_INVALID_ARG || s) return 4;
+    printf("%u %u %u %s\n", c.nx, c.ny, c.struct_size, pflbm_last_error());
+    return 0;
+}
+''')
+    exe = tmp_path / "abi"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                        "-L", str(lib.parent), "-lpflbm", f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert "nz >= 12" in r.stdout
