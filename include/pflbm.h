@@ -226,6 +226,19 @@ int pflbm_reduce_fields_noalloc(const float *rho, const float *ux, const float *
 /* Writes <dir>/<name><step:06>.bin for each field and <dir>/step_<step:06>.vti
  * that appends them (src/postProcess/PostProcess.cuh:43-261). */
 int pflbm_write_output(pflbm_sim *sim, const char *dir, const int32_t *field_ids, int32_t n_fields);
+/* Divergence watchdog (the reference aborts only on CUDA errors): with
+ * interval > 0, pflbm_step runs the FP64 diagnostics after every multiple of
+ * interval steps and returns PFLBM_ERR_DIVERGED when rho, u or phi hold
+ * NaN/Inf, or, with max_phi_mass_drift > 0, when the phi mass moved by more
+ * than that relative amount from its value at this call (closed boxes only:
+ * the jet's inflow changes the mass). interval 0 switches it off. */
+int pflbm_set_watchdog(pflbm_sim *sim, uint64_t interval, double max_phi_mass_drift);
+
+/* Same files, written by a background thread: the fields are copied to
+ * page-locked staging buffers before the call returns, so stepping can
+ * continue at once. The next write_output call, pflbm_synchronize and
+ * pflbm_destroy wait for the writer and report its I/O errors. */
+int pflbm_write_output_async(pflbm_sim *sim, const char *dir, const int32_t *field_ids, int32_t n_fields);
 
 /* Checkpoint and resume (the reference has none; its .bin dumps are
  * output only, src/main.cu:130-133). The file holds the configuration, the

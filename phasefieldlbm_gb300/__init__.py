@@ -161,6 +161,8 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_reduce": ([vp, ctypes.POINTER(Diag)], ctypes.c_int),
         "pflbm_reduce_fields_noalloc": ([vp, vp, vp, vp, vp, i32, i32, i32, vp, vp], ctypes.c_int),
         "pflbm_write_output": ([vp, ctypes.c_char_p, ctypes.POINTER(i32), i32], ctypes.c_int),
+        "pflbm_write_output_async": ([vp, ctypes.c_char_p, ctypes.POINTER(i32), i32], ctypes.c_int),
+        "pflbm_set_watchdog": ([vp, u64, ctypes.c_double], ctypes.c_int),
         "pflbm_device_bytes": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
         "pflbm_save_checkpoint": ([vp, ctypes.c_char_p], ctypes.c_int),
         "pflbm_load_checkpoint": ([vp, ctypes.c_char_p], ctypes.c_int),
@@ -450,9 +452,13 @@ class Simulation:
             _check(self.lib, rc)
         return d
 
-    def write_output(self, directory: str, fields=("rho", "uz")):
+    def write_output(self, directory: str, fields=("rho", "uz"), wait: bool = True):
+        """<field><step06>.bin + step_<step06>.vti; wait=False returns once the
+        fields are staged and writes the files in the background (finished
+        by synchronize() or the next write_output)."""
         ids = (ctypes.c_int32 * len(fields))(*[FIELD_ID[f] for f in fields])
-        _check(self.lib, self.lib.pflbm_write_output(self._h, str(directory).encode(), ids, len(fields)))
+        fn = self.lib.pflbm_write_output if wait else self.lib.pflbm_write_output_async
+        _check(self.lib, fn(self._h, str(directory).encode(), ids, len(fields)))
 
     def save_checkpoint(self, path):
         _check(self.lib, self.lib.pflbm_save_checkpoint(self._h, str(path).encode()))
@@ -477,6 +483,10 @@ class Simulation:
         v = ctypes.c_int32()
         _check(self.lib, self.lib.pflbm_kernels_per_step(self._h, ctypes.byref(v)))
         return int(v.value)
+
+    def set_watchdog(self, interval: int, max_phi_mass_drift: float = 0.0):
+        """FP64 NaN/Inf (and phi-mass drift) checks every `interval` steps of step()."""
+        _check(self.lib, self.lib.pflbm_set_watchdog(self._h, int(interval), float(max_phi_mass_drift)))
 
     def set_closure(self, blob, strength: float = 1.0):
         """Attaches a closure network (PFLBM_MLP_BLOB floats; None detaches)."""

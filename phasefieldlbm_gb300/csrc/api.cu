@@ -18,7 +18,10 @@
 #include <memory>
 #include <string>
 #include <sys/stat.h>
+#include <thread>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/pflbm.h"
 #include "engine.h"
@@ -30,6 +33,15 @@ using pflbm::HostParams;
 namespace {
 
 thread_local std::string g_err;
+
+// NVTX range around a C-ABI call (visible in Nsight timelines; no cost
+// without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 int fail(int code, const std::string &msg) {
     g_err = msg;
@@ -65,6 +77,14 @@ struct pflbm_sim {
     int64_t cache_step = -1; // step the analysis cache describes
     bool distros_dirty = false; // initial fields changed since the last rebuild
     double *dev_diag = nullptr;
+    // background output writer (pflbm_write_output_async)
+    std::thread writer;
+    int writer_rc = 0;
+    std::string writer_err;
+    std::vector<float *> pinned;  // page-locked staging, one N-float array per field
+    // divergence watchdog (pflbm_set_watchdog)
+    uint64_t wd_interval = 0;
+    double wd_max_drift = 0.0, wd_mass0 = 0.0;
 };
 
 namespace pflbm {
@@ -347,6 +367,68 @@ int sim_view(pflbm_sim *s, SimView &v) {
 }
 }  // namespace pflbm
 
+namespace {
+
+// Files of one output step: <name><step06>.bin per field (PostProcess.cuh:43-97)
+// and step_<step06>.vti, VTK ImageData with the arrays appended raw behind
+// UInt32 size headers (PostProcess.cuh:99-261). Runs on the writer thread.
+int write_step_files(const std::string &d, const std::string &suffix, const std::vector<std::string> &names,
+                     const std::vector<const float *> &data, uint64_t N, uint32_t nx, uint32_t ny, uint32_t nz,
+                     std::string &err) {
+    const uint64_t nbytes = N * sizeof(float);
+    for (size_t i = 0; i < names.size(); ++i) {
+        const std::string path = d + names[i] + suffix + ".bin";
+        std::ofstream o(path, std::ios::binary | std::ios::trunc);
+        if (!o) { err = "cannot open " + path; return PFLBM_ERR_IO; }
+        o.write(reinterpret_cast<const char *>(data[i]), std::streamsize(nbytes));
+        if (!o) { err = "write failed: " + path; return PFLBM_ERR_IO; }
+    }
+    if (names.empty()) return PFLBM_OK;
+    const std::string vti = d + "step_" + suffix + ".vti";
+    std::ofstream v(vti, std::ios::binary | std::ios::trunc);
+    if (!v) { err = "cannot open " + vti; return PFLBM_ERR_IO; }
+    v << "<?xml version=\"1.0\"?>\n";
+    v << "<VTKFile type=\"ImageData\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+    v << "  <ImageData WholeExtent=\"0 " << (nx - 1) << " 0 " << (ny - 1) << " 0 " << (nz - 1)
+      << "\" Origin=\"0 0 0\" Spacing=\"1 1 1\">\n";
+    v << "    <Piece Extent=\"0 " << (nx - 1) << " 0 " << (ny - 1) << " 0 " << (nz - 1) << "\">\n";
+    v << "      <PointData Scalars=\"" << names.front() << "\">\n";
+    uint64_t offset = 0;
+    for (const auto &name : names) {
+        v << "        <DataArray type=\"Float32\" Name=\"" << name
+          << "\" NumberOfComponents=\"1\" format=\"appended\" offset=\"" << offset << "\"/>\n";
+        offset += sizeof(uint32_t) + nbytes;
+    }
+    v << "      </PointData>\n      <CellData/>\n    </Piece>\n  </ImageData>\n";
+    v << "  <AppendedData encoding=\"raw\">\n_";
+    for (size_t i = 0; i < names.size(); ++i) {
+        const uint32_t n32 = static_cast<uint32_t>(nbytes);
+        v.write(reinterpret_cast<const char *>(&n32), sizeof n32);
+        v.write(reinterpret_cast<const char *>(data[i]), std::streamsize(nbytes));
+    }
+    v << "\n  </AppendedData>\n</VTKFile>\n";
+    if (!v) { err = "write failed: " + vti; return PFLBM_ERR_IO; }
+    return PFLBM_OK;
+}
+
+// Waits for the previous background write; reports its failure once.
+int join_writer(pflbm_sim *s) {
+    if (s->writer.joinable()) s->writer.join();
+    if (s->writer_rc) {
+        const int rc = s->writer_rc;
+        s->writer_rc = 0;
+        return fail(rc, s->writer_err);
+    }
+    return PFLBM_OK;
+}
+
+void free_pinned(pflbm_sim *s) {
+    for (float *p : s->pinned) cudaFreeHost(p);
+    s->pinned.clear();
+}
+
+}  // namespace
+
 extern "C" {
 
 int pflbm_abi_version(void) { return PFLBM_ABI_VERSION; }
@@ -396,6 +478,7 @@ int pflbm_config_reference(pflbm_config *c, int32_t flow_case, int32_t velocity_
 }
 
 int pflbm_create(const pflbm_config *cfg, pflbm_sim **out) {
+    NvtxRange nvtx_("pflbm_create");
     if (!cfg || !out) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
     int rc = validate(*cfg);
@@ -449,6 +532,7 @@ int pflbm_create(const pflbm_config *cfg, pflbm_sim **out) {
 }
 
 int pflbm_init(pflbm_sim *s) {
+    NvtxRange nvtx_("pflbm_init");
     if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
     cudaSetDevice(s->device);
     s->eng->reset_counters(s->stream);
@@ -489,6 +573,7 @@ int pflbm_set_initial_field(pflbm_sim *s, int32_t id, const float *src, size_t b
 }
 
 int pflbm_step_async(pflbm_sim *s, uint64_t n) {
+    NvtxRange nvtx_("pflbm_step");
     if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
     if (!s->initialized) return fail(PFLBM_ERR_STATE, "pflbm_init has not been called");
     cudaSetDevice(s->device);
@@ -513,16 +598,60 @@ int pflbm_synchronize(pflbm_sim *s) {
     if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
-    return check_device_error(s);
+    int rc = check_device_error(s);
+    if (rc) return rc;
+    return join_writer(s);
 }
 
 int pflbm_step(pflbm_sim *s, uint64_t n) {
-    int rc = pflbm_step_async(s, n);
-    if (rc) return rc;
-    return pflbm_synchronize(s);
+    if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
+    if (s->wd_interval == 0) {
+        int rc = pflbm_step_async(s, n);
+        if (rc) return rc;
+        return pflbm_synchronize(s);
+    }
+    // watchdog: FP64 diagnostics at every multiple of the interval
+    uint64_t left = n;
+    while (left > 0) {
+        const uint64_t k = std::min<uint64_t>(left, s->wd_interval - s->step % s->wd_interval);
+        int rc = pflbm_step_async(s, k);
+        if (rc) return rc;
+        left -= k;
+        rc = pflbm_synchronize(s);
+        if (rc) return rc;
+        if (s->step % s->wd_interval == 0) {
+            pflbm_diag d;
+            rc = pflbm_reduce(s, &d);  // PFLBM_ERR_DIVERGED on NaN/Inf
+            if (rc) return rc;
+            if (s->wd_max_drift > 0.0 && s->wd_mass0 != 0.0) {
+                const double drift = std::fabs(d.phi_mass / s->wd_mass0 - 1.0);
+                if (drift > s->wd_max_drift)
+                    return fail(PFLBM_ERR_DIVERGED, "phi mass drift " + std::to_string(drift) + " at step " +
+                                                        std::to_string(s->step) + " exceeds " +
+                                                        std::to_string(s->wd_max_drift));
+            }
+        }
+    }
+    return PFLBM_OK;
+}
+
+int pflbm_set_watchdog(pflbm_sim *s, uint64_t interval_steps, double max_phi_mass_drift) {
+    if (!s || max_phi_mass_drift < 0.0) return fail(PFLBM_ERR_INVALID_ARG, "bad argument");
+    if (!s->initialized) return fail(PFLBM_ERR_STATE, "pflbm_init has not been called");
+    s->wd_interval = interval_steps;
+    s->wd_max_drift = max_phi_mass_drift;
+    s->wd_mass0 = 0.0;
+    if (interval_steps > 0 && max_phi_mass_drift > 0.0) {
+        pflbm_diag d;
+        const int rc = pflbm_reduce(s, &d);
+        if (rc) return rc;
+        s->wd_mass0 = d.phi_mass;
+    }
+    return PFLBM_OK;
 }
 
 int pflbm_step_profiled(pflbm_sim *s, uint64_t n, double *total_ms, double *kernel_ms, int32_t nk) {
+    NvtxRange nvtx_("pflbm_step_profiled");
     if (!s || !total_ms || (nk > 0 && !kernel_ms)) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
     if (!s->initialized) return fail(PFLBM_ERR_STATE, "pflbm_init has not been called");
     cudaSetDevice(s->device);
@@ -579,6 +708,7 @@ int pflbm_get_field_f64(pflbm_sim *s, int32_t id, double *host, size_t bytes) {
 }
 
 int pflbm_reduce(pflbm_sim *s, pflbm_diag *d) {
+    NvtxRange nvtx_("pflbm_reduce");
     if (!s || !d) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
     if (!s->initialized) return fail(PFLBM_ERR_STATE, "pflbm_init has not been called");
     cudaSetDevice(s->device);
@@ -640,65 +770,51 @@ int pflbm_set_closure(pflbm_sim *s, const float *blob, float strength) {
 }
 
 
-int pflbm_write_output(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
+int pflbm_write_output_async(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
+    NvtxRange nvtx_("pflbm_write_output");
     if (!s || !dir || (!ids && n > 0) || n < 0) return fail(PFLBM_ERR_INVALID_ARG, "bad argument");
+    for (int i = 0; i < n; ++i)
+        if (ids[i] < 0 || ids[i] >= PFLBM_FIELD_COUNT) return fail(PFLBM_ERR_INVALID_ARG, "bad field id");
+    int rc = join_writer(s);  // the staging buffers are free again
+    if (rc) return rc;
     std::string d(dir);
     if (!d.empty() && d.back() != '/') d.push_back('/');
     if (!make_dirs(d)) return fail(PFLBM_ERR_IO, "cannot create " + d);
     const uint64_t N = s->hp.N;
-    const std::string suffix = step6(s->step > 0 ? s->step - 1 : 0);
-    std::vector<float> h(N);
-    struct Arr {
-        std::string name, path;
-    };
-    std::vector<Arr> arrays;
-    // <name><step06>.bin (PostProcess.cuh:43-97)
-    for (int i = 0; i < n; ++i) {
-        int rc = pflbm_get_field(s, ids[i], h.data(), N * sizeof(float));
-        if (rc) return rc;
-        const std::string path = d + kFieldNames[ids[i]] + suffix + ".bin";
-        std::ofstream o(path, std::ios::binary | std::ios::trunc);
-        if (!o) return fail(PFLBM_ERR_IO, "cannot open " + path);
-        o.write(reinterpret_cast<const char *>(h.data()), std::streamsize(N * sizeof(float)));
-        if (!o) return fail(PFLBM_ERR_IO, "write failed: " + path);
-        arrays.push_back({kFieldNames[ids[i]], path});
-    }
-    if (arrays.empty()) return PFLBM_OK;
-    // step_<step06>.vti: VTK ImageData, appended raw data with UInt32 size
-    // headers (PostProcess.cuh:99-261)
-    const std::string vti = d + "step_" + suffix + ".vti";
-    std::ofstream v(vti, std::ios::binary | std::ios::trunc);
-    if (!v) return fail(PFLBM_ERR_IO, "cannot open " + vti);
-    const uint64_t nbytes = N * sizeof(float);
-    v << "<?xml version=\"1.0\"?>\n";
-    v << "<VTKFile type=\"ImageData\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
-    v << "  <ImageData WholeExtent=\"0 " << (s->hp.nx - 1) << " 0 " << (s->hp.ny - 1) << " 0 " << (s->hp.nz - 1)
-      << "\" Origin=\"0 0 0\" Spacing=\"1 1 1\">\n";
-    v << "    <Piece Extent=\"0 " << (s->hp.nx - 1) << " 0 " << (s->hp.ny - 1) << " 0 " << (s->hp.nz - 1) << "\">\n";
-    v << "      <PointData Scalars=\"" << arrays.front().name << "\">\n";
-    uint64_t offset = 0;
-    for (auto &a : arrays) {
-        v << "        <DataArray type=\"Float32\" Name=\"" << a.name
-          << "\" NumberOfComponents=\"1\" format=\"appended\" offset=\"" << offset << "\"/>\n";
-        offset += sizeof(uint32_t) + nbytes;
-    }
-    v << "      </PointData>\n      <CellData/>\n    </Piece>\n  </ImageData>\n";
-    v << "  <AppendedData encoding=\"raw\">\n_";
-    std::vector<char> buf(1 << 20);
-    for (auto &a : arrays) {
-        const uint32_t n32 = static_cast<uint32_t>(nbytes);
-        v.write(reinterpret_cast<const char *>(&n32), sizeof n32);
-        std::ifstream in(a.path, std::ios::binary);
-        if (!in) return fail(PFLBM_ERR_IO, "cannot reopen " + a.path);
-        while (in) {
-            in.read(buf.data(), std::streamsize(buf.size()));
-            const std::streamsize got = in.gcount();
-            if (got > 0) v.write(buf.data(), got);
+    cudaSetDevice(s->device);
+    while (s->pinned.size() < size_t(n)) {
+        float *p = nullptr;
+        if (cudaMallocHost(&p, N * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(PFLBM_ERR_OUT_OF_MEMORY, "cudaMallocHost (output staging)");
         }
+        s->pinned.push_back(p);
     }
-    v << "\n  </AppendedData>\n</VTKFile>\n";
-    if (!v) return fail(PFLBM_ERR_IO, "write failed: " + vti);
+    // device -> page-locked host copies now (the analysis of the last step
+    // runs once); the file writes overlap with whatever the caller does next
+    std::vector<std::string> names;
+    std::vector<const float *> data;
+    for (int i = 0; i < n; ++i) {
+        rc = pflbm_get_field(s, ids[i], s->pinned[i], N * sizeof(float));
+        if (rc) return rc;
+        names.push_back(kFieldNames[ids[i]]);
+        data.push_back(s->pinned[i]);
+    }
+    const std::string suffix = step6(s->step > 0 ? s->step - 1 : 0);
+    const uint32_t nx = s->hp.nx, ny = s->hp.ny, nz = s->hp.nz;
+    s->writer = std::thread([s, d, suffix, names, data, N, nx, ny, nz]() {
+        std::string err;
+        const int r = write_step_files(d, suffix, names, data, N, nx, ny, nz, err);
+        s->writer_err = err;
+        s->writer_rc = r;
+    });
     return PFLBM_OK;
+}
+
+int pflbm_write_output(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
+    int rc = pflbm_write_output_async(s, dir, ids, n);
+    if (rc) return rc;
+    return join_writer(s);
 }
 
 // Checkpoint file: header, both ping-pong population buffers (the one the
@@ -823,6 +939,8 @@ int pflbm_destroy(pflbm_sim *s) {
     if (!s) return PFLBM_OK;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->writer.joinable()) s->writer.join();
+    free_pinned(s);
     destroy_graphs(s);
     if (s->dev_diag) cudaFree(s->dev_diag);
     s->eng.reset();

@@ -171,11 +171,10 @@ int main(int argc, char **argv) {
         done += n;
         step = next_out + 1;
         if (!benchmark) {
-            rc = pflbm_synchronize(sim);
-            if (rc) return die("pflbm_synchronize", rc);
+            // the files are written in the background while the next steps run
             std::printf("Step %ld: bins in %s\n", done - 1, dir.c_str());
-            rc = pflbm_write_output(sim, dir.c_str(), fields.data(), int32_t(fields.size()));
-            if (rc) return die("pflbm_write_output", rc);
+            rc = pflbm_write_output_async(sim, dir.c_str(), fields.data(), int32_t(fields.size()));
+            if (rc) return die("pflbm_write_output_async", rc);
         }
     }
     rc = pflbm_synchronize(sim);

@@ -75,6 +75,20 @@ class EngineT final : public Engine {
             {reinterpret_cast<void **>(&err_), sizeof(unsigned int) * 4},
             {reinterpret_cast<void **>(&partial_), sizeof(double) * RED_FIELDS * kRedBlocks},
         };
+        // fault injection on the host: PFLBM_ALLOC_LIMIT_BYTES caps the
+        // device bytes one simulation may take (allocation fails cleanly)
+        uint64_t planned = 0;
+        for (auto &r : reqs) planned += r.bytes;
+        if (flags_ & (PFLBM_FLAG_TIME_AVERAGE | PFLBM_FLAG_REYNOLDS_MOMENTS)) planned += sizeof(T) * 10 * N;
+        if (flags_ & PFLBM_FLAG_VORTICITY) planned += sizeof(T) * 4 * N;
+        if (const char *lim = std::getenv("PFLBM_ALLOC_LIMIT_BYTES")) {
+            const unsigned long long cap = std::strtoull(lim, nullptr, 10);
+            if (cap > 0 && planned > cap) {
+                err = "device allocation of " + std::to_string(planned) + " bytes exceeds PFLBM_ALLOC_LIMIT_BYTES=" +
+                      std::to_string(cap);
+                return PFLBM_ERR_OUT_OF_MEMORY;
+            }
+        }
         for (auto &r : reqs) {
             if (cudaMalloc(r.ptr, r.bytes) != cudaSuccess) {
                 cudaGetLastError();

@@ -36,3 +36,22 @@ def test_pipeline_writes_reference_layout(pflbm):
             ref = s.get_field(f).reshape(-1)
             got = np.fromfile(out / f"{f}000020.bin", np.float32)
             assert np.array_equal(got, ref), f
+
+
+def test_async_output_matches_sync(pflbm, tmp_path):
+    """pflbm_write_output_async stages the fields before returning; stepping
+    on while the writer thread runs leaves the written step unchanged."""
+    cfg = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
+    cfg.nx, cfg.ny, cfg.nz, cfg.diam, cfg.radius = 32, 32, 48, 8, 4
+    fields = ("rho", "uz", "phi")
+    with pflbm.Simulation(cfg) as s:
+        s.step(11)
+        s.write_output(tmp_path / "sync", fields)
+        s.write_output(tmp_path / "async", fields, wait=False)
+        s.step(7)  # runs while the files are written
+        s.synchronize()
+    for f in fields:
+        a = (tmp_path / "sync" / f"{f}000010.bin").read_bytes()
+        b = (tmp_path / "async" / f"{f}000010.bin").read_bytes()
+        assert a == b and len(a) == 4 * 32 * 32 * 48, f
+    assert (tmp_path / "sync" / "step_000010.vti").read_bytes() == (tmp_path / "async" / "step_000010.vti").read_bytes()
