@@ -64,9 +64,13 @@ struct TmaPlan {
 
 // Deepest pipeline (4, 3 or 2 stages) that keeps two CTAs per SM (FP32 and
 // 16-bit storage: <= 113 KB each) or one (FP64: <= 227 KB).
+#ifndef PFLBM_TMA_SMEM_BUDGET
+#define PFLBM_TMA_SMEM_BUDGET (113u * 1024u)  // per CTA: two CTAs per SM
+#endif
+
 template <int QQ, class S>
 struct TmaStages {
-    static constexpr size_t kBudget = sizeof(typename Store<S>::T) == 8 ? 227u * 1024u : 113u * 1024u;
+    static constexpr size_t kBudget = sizeof(typename Store<S>::T) == 8 ? 227u * 1024u : size_t(PFLBM_TMA_SMEM_BUDGET);
     static constexpr int value = TmaPlan<QQ, S, 4>::total <= kBudget   ? 4
                                  : TmaPlan<QQ, S, 3>::total <= kBudget ? 3
                                                                        : 2;
