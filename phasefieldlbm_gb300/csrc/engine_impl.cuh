@@ -49,6 +49,47 @@ Params<T> make_params(const HostParams &h) {
     return p;
 }
 
+// Tensor maps of the TMA collide kernel for one grid: f as (x, y, z, q) with
+// boxes (BW, TY, 1, 1), phi as (x, y, z) with boxes (PBW, PBH, 1). False when
+// the driver entry point is missing or the encoder rejects the layout.
+template <int QQ, class S>
+bool encode_collide_maps(const S *f, const typename Store<S>::T *phi, uint64_t nx, uint64_t ny, uint64_t nz,
+                         CUtensorMap &fmap, CUtensorMap &phimap) {
+    using T = typename Store<S>::T;
+    using L = TmaLayout<QQ, S>;
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return false;
+    }
+    Encode enc = reinterpret_cast<Encode>(fn);
+    const CUtensorMapDataType ft = std::is_same<S, float>::value    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                   : std::is_same<S, double>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                   : std::is_same<S, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                    : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    const CUtensorMapDataType pt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const uint64_t N = nx * ny * nz;
+    const cuuint64_t fdim[4] = {nx, ny, nz, cuuint64_t(QQ)};
+    const cuuint64_t fstr[3] = {nx * sizeof(S), nx * ny * sizeof(S), N * sizeof(S)};
+    const cuuint32_t fbox[4] = {cuuint32_t(L::BW), cuuint32_t(TY), 1, 1};
+    const cuuint32_t one4[4] = {1, 1, 1, 1};
+    if (enc(&fmap, ft, 4, const_cast<S *>(f), fdim, fstr, fbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t pdim[3] = {nx, ny, nz};
+    const cuuint64_t pstr[2] = {nx * sizeof(T), nx * ny * sizeof(T)};
+    const cuuint32_t pbox[3] = {cuuint32_t(L::PBW), cuuint32_t(L::PBH), 1};
+    return enc(&phimap, pt, 3, const_cast<T *>(phi), pdim, pstr, pbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int QQ, bool JET, class S>
 class EngineT final : public Engine {
     using T = typename Store<S>::T;
@@ -136,41 +177,8 @@ class EngineT final : public Engine {
             if (e[0] == '1') return;
         if ((uint64_t(h_.nx) * sizeof(S)) % 16 != 0 || (uint64_t(h_.nx) * sizeof(T)) % 16 != 0) return;
         using L = TmaLayout<QQ, S>;
-        using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess || !fn) {
-            cudaGetLastError();
-            return;
-        }
-        Encode enc = reinterpret_cast<Encode>(fn);
-        CUtensorMapDataType ft = std::is_same<S, float>::value    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                 : std::is_same<S, double>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
-                                 : std::is_same<S, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                                                  : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-        CUtensorMapDataType pt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-        const uint64_t nx = h_.nx, ny = h_.ny, nz = h_.nz, N = h_.N;
-        for (int k = 0; k < 2; ++k) {
-            const cuuint64_t fdim[4] = {nx, ny, nz, cuuint64_t(QQ)};
-            const cuuint64_t fstr[3] = {nx * sizeof(S), nx * ny * sizeof(S), N * sizeof(S)};
-            const cuuint32_t fbox[4] = {cuuint32_t(L::BW), cuuint32_t(TY), 1, 1};
-            const cuuint32_t one4[4] = {1, 1, 1, 1};
-            if (enc(&fmap_[k], ft, 4, f_[k], fdim, fstr, fbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-                return;
-            const cuuint64_t pdim[3] = {nx, ny, nz};
-            const cuuint64_t pstr[2] = {nx * sizeof(T), nx * ny * sizeof(T)};
-            const cuuint32_t pbox[3] = {cuuint32_t(L::PBW), cuuint32_t(L::PBH), 1};
-            if (enc(&phimap_[k], pt, 3, phi_[k], pdim, pstr, pbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-                return;
-        }
+        for (int k = 0; k < 2; ++k)
+            if (!encode_collide_maps<QQ, S>(f_[k], phi_[k], h_.nx, h_.ny, h_.nz, fmap_[k], phimap_[k])) return;
         if (cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(L::total)) != cudaSuccess ||
             cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_AVG>,

@@ -5,7 +5,8 @@
 // All boxes live in shared allocations (per-box offsets). One time step is
 // two persistent launches covering every box: a fixed grid of CTAs pulls
 // work items (box, 32x8 column tile, z chunk) from a device counter and runs
-// the same tile code as the single-box collide and phase kernels. Chunks of
+// the same tile code as the single-box collide and phase kernels (TMA-fed
+// when every box's rows are 16-byte aligned). Chunks of
 // steps are captured into CUDA graphs. The z-chunk length and the number of
 // resident CTAs per SM are chosen by a measured autotuner.
 #include <algorithm>
@@ -78,6 +79,43 @@ __global__ void __launch_bounds__(NT, 2)
     }
 }
 
+// TMA-fed variant of k_collide_batch: the tile code of k_collide_tma on
+// per-box tensor maps (kernel parameter, for the launch's parity). The CTA's
+// pipeline barriers carry on from tile to tile through `seq`.
+constexpr int kMaxTmaBoxes = 64;
+struct BatchMaps {
+    CUtensorMap f[kMaxTmaBoxes];
+    CUtensorMap phi[kMaxTmaBoxes];
+};
+
+template <int QQ>
+__global__ void __launch_bounds__(NT, 2)
+    k_collide_batch_tma(const __grid_constant__ BatchMaps maps, const BoxDev *boxes, const WorkItem *items,
+                        int n_items, BatchPtrs bp, int parity) {
+    using L = TmaLayout<QQ, float>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    static_assert(8 * L::kStages + 4 <= 64, "item slot after the barriers");
+    volatile int *s_item = reinterpret_cast<volatile int *>(smem + L::off_bar + 64);
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    if (blockIdx.x == 0 && tid == 0) bp.ctr[1] = 0u;
+    tma_pipeline_init<QQ, float>(smem);
+    uint32_t seq = 0;
+    for (;;) {
+        if (tid == 0) *s_item = int(atomicAdd(&bp.ctr[0], 1u));
+        __syncthreads();
+        const int it = *s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const WorkItem w = items[it];
+        const BoxDev &bx = boxes[w.box];
+        const StepBuffers<float, float> b = box_buffers(bp, bx, parity);
+        if (!collide_tile_tma<QQ, false, float, MODE_STEP>(bx.p, b, &maps.f[w.box], &maps.phi[w.box], w.x0, w.y0,
+                                                          w.zb, w.ze, smem, seq))
+            return;
+        __syncthreads();  // shared rings are reused by the next item
+    }
+}
+
 // Persistent phase step over the same work items; advances the step counter
 // and resets the collide kernel's work counter.
 template <int QQ>
@@ -127,6 +165,8 @@ class Ensemble {
     uint64_t step = 0;
     int zchunk = 16, ctas_per_sm = 2;
     bool initialized = false;
+    bool use_tma = false;
+    std::unique_ptr<BatchMaps> maps[2];  // per parity (read buffer)
     static constexpr int kChunk = 16;
     static constexpr int kRedBlocks = 304;
 
@@ -170,13 +210,56 @@ class Ensemble {
         return PFLBM_OK;
     }
 
+    // TMA maps for every box and parity when all rows are 16-byte aligned
+    // and the boxes fit the kernel-parameter table; otherwise plain loads.
+    // PFLBM_NO_TMA=1 forces plain loads.
+    void setup_tma() {
+        use_tma = false;
+        if (const char *e = std::getenv("PFLBM_NO_TMA"))
+            if (e[0] == '1') return;
+        if (boxes.size() > size_t(kMaxTmaBoxes)) return;
+        for (const auto &bx : boxes)
+            if ((uint64_t(bx.p.nx) * sizeof(float)) % 16 != 0) return;
+        for (int par = 0; par < 2; ++par) {
+            maps[par].reset(new (std::nothrow) BatchMaps());
+            if (!maps[par]) return;
+            for (size_t k = 0; k < boxes.size(); ++k) {
+                const BoxDev &bx = boxes[k];
+                const bool ok =
+                    q == 19 ? encode_collide_maps<19, float>(bp.f[par] + bx.f_off, bp.phi[par] + bx.n_off, bx.p.nx,
+                                                            bx.p.ny, bx.p.nz, maps[par]->f[k], maps[par]->phi[k])
+                            : encode_collide_maps<27, float>(bp.f[par] + bx.f_off, bp.phi[par] + bx.n_off, bx.p.nx,
+                                                            bx.p.ny, bx.p.nz, maps[par]->f[k], maps[par]->phi[k]);
+                if (!ok) return;
+            }
+        }
+        const cudaError_t e =
+            q == 19 ? cudaFuncSetAttribute(k_collide_batch_tma<19>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(TmaLayout<19, float>::total))
+                    : cudaFuncSetAttribute(k_collide_batch_tma<27>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           int(TmaLayout<27, float>::total));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        use_tma = true;
+    }
+
     void enqueue_step(int par, cudaStream_t s) {
         const int grid = std::max(1, sms * ctas_per_sm);
         if (q == 19) {
-            k_collide_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            if (use_tma)
+                k_collide_batch_tma<19><<<grid, dim3(TX, TY), TmaLayout<19, float>::total, s>>>(
+                    *maps[par], d_boxes, d_items, n_items, bp, par);
+            else
+                k_collide_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
             k_phase_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
         } else {
-            k_collide_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            if (use_tma)
+                k_collide_batch_tma<27><<<grid, dim3(TX, TY), TmaLayout<27, float>::total, s>>>(
+                    *maps[par], d_boxes, d_items, n_items, bp, par);
+            else
+                k_collide_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
             k_phase_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
         }
     }
@@ -334,6 +417,7 @@ int pflbm_ensemble_create(const pflbm_config *cfgs, int32_t n, pflbm_ensemble **
     cudaMemcpy(e->d_boxes, e->boxes.data(), sizeof(pflbm::BoxDev) * n, cudaMemcpyHostToDevice);
     ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) return ecuda(ce, "cudaStreamCreate");
+    e->setup_tma();
     int rc = e->build_items();
     if (rc) return efail(rc, "work list allocation failed");
     rc = e->capture();

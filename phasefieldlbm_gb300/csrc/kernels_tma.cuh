@@ -79,13 +79,31 @@ struct TmaStages {
 template <int QQ, class S>
 using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S>::value>;
 
+// Barriers of the TMA pipeline: once per CTA, before its first tile.
+template <int QQ, class S>
+__device__ __forceinline__ void tma_pipeline_init(unsigned char *smem) {
+    using L = TmaLayout<QQ, S>;
+    if (threadIdx.x + blockDim.x * threadIdx.y == 0) {
+        uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
+        for (int k = 0; k < L::kStages; ++k) mbar_init(&bar[k], 1);
+        *reinterpret_cast<volatile int *>(smem + L::off_bar + 8 * L::kStages) = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+// One column tile [x0, x0+TX) x [y0, y0+TY), planes zb .. ze-1. `seq` counts
+// the stages this CTA has consumed so far (stage = seq % NS, mbarrier phase
+// parity = (seq / NS) & 1), so that a persistent CTA can run tile after tile
+// on the same barriers; every stage issued for a tile is consumed by it.
+// Returns false when a bounded wait gave up (error word set, copies drained).
 template <int QQ, bool JET, class S, int MODE>
-__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : PFLBM_COLLIDE_MIN_BLOCKS))
-    k_collide_tma(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b,
-                  const __grid_constant__ CUtensorMap fmap, const __grid_constant__ CUtensorMap phimap) {
+__device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>::T> &p,
+                                                 const StepBuffers<S, typename Store<S>::T> &b,
+                                                 const CUtensorMap *fmap_p, const CUtensorMap *phimap_p, int x0,
+                                                 int y0, int zb, int ze, unsigned char *smem, uint32_t &seq) {
     using T = typename Store<S>::T;
     using L = TmaLayout<QQ, S>;
-    extern __shared__ __align__(128) unsigned char smem[];
     S *s_f = reinterpret_cast<S *>(smem + L::off_f);
     T *s_phi = reinterpret_cast<T *>(smem + L::off_phi);
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);
@@ -95,10 +113,7 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
 
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TX * ty;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const int x = x0 + tx, y = y0 + ty;
-    const int zb = 1 + blockIdx.z * p.zchunk;
-    const int ze = min(zb + p.zchunk, nz - 1);
     const bool col = (x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2);
     const uint32_t t = b.step_in ? static_cast<uint32_t>(*b.step_in) : b.t_fixed;
 
@@ -116,18 +131,14 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
         unsigned char *dst = reinterpret_cast<unsigned char *>(s_f) + size_t(stage) * L::stage_bytes;
 #pragma unroll
         for (int q = 0; q < QQ; ++q)
-            tma_load_4d(dst + size_t(q) * L::box_stride, &fmap, &bar[stage], x0 - L::XO, y0 - kCY[q], zf - kCZ[q], q);
-        tma_load_3d(&phi_at(pslot(zf + 2), 0, 0), &phimap, &bar[stage], x0 - L::PXO, y0 - 2, zf + 2);
+            tma_load_4d(dst + size_t(q) * L::box_stride, fmap_p, &bar[stage], x0 - L::XO, y0 - kCY[q], zf - kCZ[q], q);
+        tma_load_3d(&phi_at(pslot(zf + 2), 0, 0), phimap_p, &bar[stage], x0 - L::PXO, y0 - 2, zf + 2);
     };
 
     if (tid == 0) {
-        tma_prefetch_desc(&fmap);
-        tma_prefetch_desc(&phimap);
-        for (int k = 0; k < NS; ++k) mbar_init(&bar[k], 1);
-        *s_abort = 0;
-        fence_mbar_init();
+        tma_prefetch_desc(fmap_p);
+        tma_prefetch_desc(phimap_p);
     }
-    __syncthreads();
 
     // warm-up: phi planes zb-2 .. zb+1 with plain loads, normals of zb-1, zb
     for (int zp = zb - 2; zp <= zb + 1; ++zp) {
@@ -141,6 +152,8 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
             phi_at(slot, ly, lx) = v;
         }
     }
+    // these generic writes precede later TMA writes to the same ring slots
+    fence_proxy_async();
     auto compute_n = [&](int zp) {
         const int sn = pslot(zp), sm = pslot(zp - 1), sp = pslot(zp + 1);
         const int nn = (zp + 4) & 3;  // normal ring slot
@@ -173,12 +186,13 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
     // stages 0 .. NS-2 (planes zb .., phi zb+2 ..); the phi ring slot of
     // plane zb+NS aliases that of zb-2, which compute_n(zb-1) no longer needs
     if (tid == 0)
-        for (int k = 0; k < NS - 1 && zb + k < ze; ++k) issue(k, zb + k);
+        for (int k = 0; k < NS - 1 && zb + k < ze; ++k) issue((seq + k) % NS, zb + k);
     compute_n(zb);
 
-    for (int z = zb, it = 0; z < ze; ++z, ++it) {
-        const int st = it % NS;
-        const uint32_t par = (it / NS) & 1;
+    for (int z = zb; z < ze; ++z) {
+        const uint32_t sq = seq + uint32_t(z - zb);
+        const int st = int(sq % NS);
+        const uint32_t par = (sq / NS) & 1;
         if (!mbar_wait_bounded(&bar[st], par, kWaitLimit)) *s_abort = 1;
         compute_n(z + 1);
         __syncthreads();
@@ -187,12 +201,12 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
                 atomicOr(b.err, 1u);
                 // drain this CTA's own copies still in flight (planes z .. z+NS-2)
                 for (int k = 0; k < NS - 1 && z + k < ze; ++k)
-                    mbar_wait_bounded(&bar[(it + k) % NS], ((it + k) / NS) & 1, kWaitLimit);
+                    mbar_wait_bounded(&bar[(sq + k) % NS], ((sq + k) / NS) & 1, kWaitLimit);
             }
-            return;
+            return false;
         }
         // plane z+NS-1 goes into the stage of plane z-1, consumed last iteration
-        if (tid == 0 && z + NS - 1 < ze) issue((it + NS - 1) % NS, z + NS - 1);
+        if (tid == 0 && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
         if (!col) continue;
 
         const int s_m = (z + 3) & 3, s_0 = z & 3, s_p = (z + 1) & 3;
@@ -215,6 +229,21 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
                                      static_cast<T>(weight<QQ>(q)));
         collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature);
     }
+    seq += uint32_t(ze - zb);
+    return true;
+}
+
+template <int QQ, bool JET, class S, int MODE>
+__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : PFLBM_COLLIDE_MIN_BLOCKS))
+    k_collide_tma(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b,
+                  const __grid_constant__ CUtensorMap fmap, const __grid_constant__ CUtensorMap phimap) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    tma_pipeline_init<QQ, S>(smem);
+    const int zb = 1 + blockIdx.z * p.zchunk;
+    const int ze = min(zb + p.zchunk, int(p.nz) - 1);
+    uint32_t seq = 0;
+    collide_tile_tma<QQ, JET, S, MODE>(p, b, &fmap, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb, ze, smem,
+                                       seq);
 }
 
 }  // namespace pflbm

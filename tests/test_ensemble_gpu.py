@@ -63,3 +63,22 @@ def test_autotune_and_mass(pflbm):
             d = ens.reduce(k)
             assert d.nonfinite == 0
             assert abs(d.phi_mass - m0[k]) / m0[k] < 1e-6
+
+
+@pytest.mark.parametrize("vs", [19, 27])
+def test_tma_and_plain_batch_kernels_bit_identical(pflbm, monkeypatch, vs):
+    """The TMA-fed batch collide (per-box tensor maps, pipeline barriers
+    carried from tile to tile) computes exactly what the plain-load batch
+    collide computes."""
+    cfgs = small_batch(pflbm, n=5, vs=vs)
+    out = {}
+    for mode in ("tma", "plain"):
+        if mode == "plain":
+            monkeypatch.setenv("PFLBM_NO_TMA", "1")
+        with pflbm.Ensemble(cfgs) as ens:
+            ens.set_tuning(8, 2)
+            ens.step(23)
+            out[mode] = [{f: ens.get_field(k, f) for f in FIELDS} for k in range(len(cfgs))]
+    for k in range(len(cfgs)):
+        for f in FIELDS:
+            assert np.array_equal(out["tma"][k][f], out["plain"][k][f]), (k, f)
