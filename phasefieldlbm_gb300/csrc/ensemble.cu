@@ -143,6 +143,35 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
+// Vectorised phase step over the same work items for boxes with nx % 4 == 0
+// (phase_vec4, as k_phase_v4): in a 32x8 tile, 8 threads cover a row as 4
+// float4 segments and the 4 groups of 8 take every 4th plane of the chunk.
+template <int QQ>
+__global__ void __launch_bounds__(NT)
+    k_phase_batch_v4(const BoxDev *boxes, const WorkItem *items, int n_items, BatchPtrs bp, int parity) {
+    static_assert(TX == 32, "8 float4 segments per 32-node tile row");
+    __shared__ int s_item;
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    if (blockIdx.x == 0 && tid == 0) {
+        bp.ctr[0] = 0u;
+        bp.step[parity ^ 1] = bp.step[parity] + 1ull;
+    }
+    const int seg = threadIdx.x & 7, zo = threadIdx.x >> 3;
+    for (;;) {
+        if (tid == 0) s_item = int(atomicAdd(&bp.ctr[1], 1u));
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const WorkItem w = items[it];
+        const BoxDev &bx = boxes[w.box];
+        const StepBuffers<float, float> b = box_buffers(bp, bx, parity);
+        const int x4 = w.x0 + 4 * seg, y = w.y0 + int(threadIdx.y);
+        if (x4 < int(bx.p.nx) && y >= 1 && y <= int(bx.p.ny) - 2)
+            for (int z = w.zb + zo; z < w.ze; z += 4) phase_vec4<false, float>(bx.p, b, x4, y, z);
+    }
+}
+
 class Ensemble {
    public:
     int q = 19;
@@ -166,6 +195,7 @@ class Ensemble {
     int zchunk = 16, ctas_per_sm = 2;
     bool initialized = false;
     bool use_tma = false;
+    bool use_vec = false;  // every box has nx % 4 == 0: float4 phase kernel
     std::unique_ptr<BatchMaps> maps[2];  // per parity (read buffer)
     static constexpr int kChunk = 16;
     static constexpr int kRedBlocks = 304;
@@ -215,6 +245,11 @@ class Ensemble {
     // PFLBM_NO_TMA=1 forces plain loads.
     void setup_tma() {
         use_tma = false;
+        use_vec = true;
+        for (const auto &bx : boxes)
+            if (bx.p.nx % 4 != 0) use_vec = false;
+        if (const char *e = std::getenv("PFLBM_NO_VEC"))
+            if (e[0] == '1') use_vec = false;
         if (const char *e = std::getenv("PFLBM_NO_TMA"))
             if (e[0] == '1') return;
         if (boxes.size() > size_t(kMaxTmaBoxes)) return;
@@ -253,14 +288,20 @@ class Ensemble {
                     *maps[par], d_boxes, d_items, n_items, bp, par);
             else
                 k_collide_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
-            k_phase_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            if (use_vec)
+                k_phase_batch_v4<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            else
+                k_phase_batch<19><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
         } else {
             if (use_tma)
                 k_collide_batch_tma<27><<<grid, dim3(TX, TY), TmaLayout<27, float>::total, s>>>(
                     *maps[par], d_boxes, d_items, n_items, bp, par);
             else
                 k_collide_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
-            k_phase_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            if (use_vec)
+                k_phase_batch_v4<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
+            else
+                k_phase_batch<27><<<grid, dim3(TX, TY), 0, s>>>(d_boxes, d_items, n_items, bp, par);
         }
     }
 

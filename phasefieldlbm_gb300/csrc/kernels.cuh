@@ -796,35 +796,14 @@ __device__ __noinline__ void phase_node_outlined(const Params<float> &p, const S
     phase_node<QQ, JET, S>(p, b, x, y, z, t);
 }
 
-// FP32 phase step with 128-bit accesses: one thread owns 4 consecutive x
-// nodes (nx % 4 == 0), reads the phi/J rows of its y and z neighbours as
-// float4 and the two x-end neighbours (periodically wrapped) as scalars.
-// The jet's boundary planes z = 1 and nz-2 go through phase_node, one node
-// per thread, in grid slices of their own.
-template <int QQ, bool JET, class S>
-__global__ void __launch_bounds__(256, 4)
-    k_phase_v4(const __grid_constant__ Params<float> p, const __grid_constant__ StepBuffers<S, float> b) {
+// The phase sum of the 4 consecutive nodes x4 .. x4+3 of row (y, z), an
+// interior row of a grid with nx % 4 == 0 (shared by k_phase_v4 and the
+// ensemble's batch phase kernel).
+template <bool JET, class S>
+__device__ __forceinline__ void phase_vec4(const Params<float> &p, const StepBuffers<S, float> &b, int x4, int y,
+                                           int z) {
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N;
-    const int x4 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint32_t t = static_cast<uint32_t>(*b.step_in);
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-        *b.step_out = *b.step_in + 1ull;
-    int z = blockIdx.z;
-    if constexpr (JET) {
-        // grid.z = nz + 4: slices 0-3 and 4-7 are the boundary planes 1 and
-        // nz-2, one node per thread (x = x4 + slice), scheduled first because
-        // their rebuilds are the longest; slices 8.. are planes 2 .. nz-3
-        if (blockIdx.z < 8) {
-            const int zb = blockIdx.z < 4 ? 1 : nz - 2;
-            const int x = x4 + (blockIdx.z & 3);
-            if (x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2) phase_node_outlined<QQ, JET, S>(p, b, x, y, zb, t);
-            return;
-        }
-        z = blockIdx.z - 6;
-    }
-    if (x4 >= nx || y < 1 || y > ny - 2 || z < 1 || z > nz - 2) return;
     const int ym = wrapi(y - 1, ny), yp = wrapi(y + 1, ny);
     const int zm = JET ? z - 1 : wrapi(z - 1, nz), zp = JET ? z + 1 : wrapi(z + 1, nz);
     auto row = [&](int yy, int zz) -> uint64_t { return static_cast<uint64_t>(nx) * (yy + static_cast<uint64_t>(ny) * zz); };
@@ -880,6 +859,37 @@ __global__ void __launch_bounds__(256, 4)
             if (x >= 1 && x <= nx - 2) b.phi_dst[r0 + x] = out[k];
         }
     }
+}
+
+// FP32 phase step with 128-bit accesses: one thread owns 4 consecutive x
+// nodes (nx % 4 == 0), reads the phi/J rows of its y and z neighbours as
+// float4 and the two x-end neighbours (periodically wrapped) as scalars.
+// The jet's boundary planes z = 1 and nz-2 go through phase_node, one node
+// per thread, in grid slices of their own.
+template <int QQ, bool JET, class S>
+__global__ void __launch_bounds__(256, 4)
+    k_phase_v4(const __grid_constant__ Params<float> p, const __grid_constant__ StepBuffers<S, float> b) {
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const int x4 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint32_t t = static_cast<uint32_t>(*b.step_in);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *b.step_out = *b.step_in + 1ull;
+    int z = blockIdx.z;
+    if constexpr (JET) {
+        // grid.z = nz + 4: slices 0-3 and 4-7 are the boundary planes 1 and
+        // nz-2, one node per thread (x = x4 + slice), scheduled first because
+        // their rebuilds are the longest; slices 8.. are planes 2 .. nz-3
+        if (blockIdx.z < 8) {
+            const int zb = blockIdx.z < 4 ? 1 : nz - 2;
+            const int x = x4 + (blockIdx.z & 3);
+            if (x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2) phase_node_outlined<QQ, JET, S>(p, b, x, y, zb, t);
+            return;
+        }
+        z = blockIdx.z - 6;
+    }
+    if (x4 >= nx || y < 1 || y > ny - 2 || z < 1 || z > nz - 2) return;
+    phase_vec4<JET, S>(p, b, x4, y, z);
 }
 
 // ------------------------------------------------------------ init

@@ -68,13 +68,14 @@ def test_autotune_and_mass(pflbm):
 @pytest.mark.parametrize("vs", [19, 27])
 def test_tma_and_plain_batch_kernels_bit_identical(pflbm, monkeypatch, vs):
     """The TMA-fed batch collide (per-box tensor maps, pipeline barriers
-    carried from tile to tile) computes exactly what the plain-load batch
-    collide computes."""
+    carried from tile to tile) and the float4 batch phase step compute
+    exactly what the plain-load collide and the scalar phase step compute."""
     cfgs = small_batch(pflbm, n=5, vs=vs)
     out = {}
     for mode in ("tma", "plain"):
         if mode == "plain":
             monkeypatch.setenv("PFLBM_NO_TMA", "1")
+            monkeypatch.setenv("PFLBM_NO_VEC", "1")
         with pflbm.Ensemble(cfgs) as ens:
             ens.set_tuning(8, 2)
             ens.step(23)
