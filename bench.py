@@ -298,7 +298,10 @@ def run_gpu(args, ranks: Ranks) -> dict:
 
     cpu = None
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
-        csteps = 2
+        # a bounded sample of about 10 s of host work: as many full-grid steps
+        # as one timed step suggests, at least 2
+        m1, d1, _ = cpu_oracle_mlups(cfg, 1)
+        csteps = max(2, min(40, int(10.0 / max(d1, 1e-3))))
         mlups, dt, cores = cpu_oracle_mlups(cfg, csteps)
         cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
                "sample": f"{csteps} time steps of the full {cfg.nx}x{cfg.ny}x{cfg.nz} D3Q{q} jet (FP32) after 1 warm-up "
