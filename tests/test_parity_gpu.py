@@ -24,6 +24,8 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 BASIC = ("rho", "ux", "uy", "uz", "phi")
+AVG_FIELDS = ("avg_phi", "avg_ux", "avg_uy", "avg_uz", "avg_uxux", "avg_uyuy", "avg_uzuz", "avg_uxuy",
+              "avg_uxuz", "avg_uyuz")
 ALL18 = ("rho", "ux", "uy", "uz", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz",
          "phi", "normx", "normy", "normz", "ind", "fsx", "fsy", "fsz")
 
@@ -202,12 +204,16 @@ def test_write_output_layout(pflbm, tmp_path):
         assert b'Name="uz" NumberOfComponents="1" format="appended" offset="16388"' in vti
 
 
-@pytest.mark.parametrize("vs,storage", [(19, 0), (27, 0), (19, 1), (27, 2), (19, 3)])
-def test_tma_and_vector_paths_bit_identical(pflbm, monkeypatch, vs, storage):
+@pytest.mark.parametrize("vs,storage,avg", [(19, 0, 0), (27, 0, 0), (19, 1, 0), (27, 2, 0), (19, 3, 0), (27, 0, 1)])
+def test_tma_and_vector_paths_bit_identical(pflbm, monkeypatch, vs, storage, avg):
     # The TMA-fed collide kernel and the float4 phase kernel compute exactly
-    # what the plain-load kernels compute; only the data movement differs.
+    # what the plain-load kernels compute; only the data movement differs
+    # (avg: the collide mode that also updates the time averages).
     c = jet_cfg(pflbm, vs, nx=64, ny=40, nz=48, diam=10, noise=1)
     c.storage = storage
+    if avg:
+        c.flags = pflbm.FLAG_TIME_AVERAGE | pflbm.FLAG_REYNOLDS_MOMENTS
+    fields = ALL18 + (AVG_FIELDS if avg else ())
     out = {}
     for mode in ("fast", "plain"):
         if mode == "plain":
@@ -219,8 +225,8 @@ def test_tma_and_vector_paths_bit_identical(pflbm, monkeypatch, vs, storage):
             else:
                 assert not s.uses_tma
             s.step(33)
-            out[mode] = {f: s.get_field(f, dtype=np.float64) for f in ALL18}
-    for f in ALL18:
+            out[mode] = {f: s.get_field(f, dtype=np.float64) for f in fields}
+    for f in fields:
         assert np.array_equal(out["fast"][f], out["plain"][f]), f
 
 
