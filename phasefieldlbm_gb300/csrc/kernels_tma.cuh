@@ -4,7 +4,7 @@
 // Same computation as k_collide (kernels.cuh), same 32x8 column tile marching
 // a chunk of z planes, but the populations of a plane are brought into
 // shared memory by the Tensor Memory Accelerator up to NS-1 planes ahead of
-// use (NS = 2..4 stages, as many as keep two CTAs per SM resident):
+// use (NS = 2..4 stages, as many as keep the CollideOccupancy CTAs resident):
 //   * f: one 4D tensor map (x, y, z, q). For plane z and direction q the CTA
 //     needs the source tile shifted by -c_q; it loads one box per direction,
 //     (32 + 2*XO) x 8 wide, whose x origin x0 - XO is 16-byte aligned, at
@@ -68,9 +68,21 @@ struct TmaPlan {
 #define PFLBM_TMA_SMEM_BUDGET (113u * 1024u)  // per CTA: two CTAs per SM
 #endif
 
+// Resident CTAs per SM of the TMA collide: one for FP64; three for D3Q19
+// with 16-bit storage, which is issue-bound rather than bandwidth-bound and
+// gains more from the extra warps (80 registers) than it loses to the
+// shallower pipeline; two otherwise.
+template <int QQ, class S>
+struct CollideOccupancy {
+    static constexpr int value =
+        sizeof(typename Store<S>::T) == 8 ? 1 : (sizeof(S) == 2 && QQ == 19 ? 3 : PFLBM_COLLIDE_MIN_BLOCKS);
+};
+
 template <int QQ, class S>
 struct TmaStages {
-    static constexpr size_t kBudget = sizeof(typename Store<S>::T) == 8 ? 227u * 1024u : size_t(PFLBM_TMA_SMEM_BUDGET);
+    static constexpr size_t kBudget = sizeof(typename Store<S>::T) == 8 ? 227u * 1024u
+                                      : CollideOccupancy<QQ, S>::value == 3 ? 74u * 1024u
+                                                                            : size_t(PFLBM_TMA_SMEM_BUDGET);
     static constexpr int value = TmaPlan<QQ, S, 4>::total <= kBudget   ? 4
                                  : TmaPlan<QQ, S, 3>::total <= kBudget ? 3
                                                                        : 2;
@@ -234,7 +246,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
 }
 
 template <int QQ, bool JET, class S, int MODE>
-__global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : PFLBM_COLLIDE_MIN_BLOCKS))
+__global__ void __launch_bounds__(NT, CollideOccupancy<QQ, S>::value)
     k_collide_tma(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b,
                   const __grid_constant__ CUtensorMap fmap, const __grid_constant__ CUtensorMap phimap) {
     extern __shared__ __align__(128) unsigned char smem[];
