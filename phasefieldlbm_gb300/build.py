@@ -88,5 +88,41 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
     return LIB
 
 
+CHECKED = BUILD / "checked"
+
+
+def build_checked(jobs: int | None = None) -> Path:
+    """A test build of the library with -DPFLBM_CHECK_BOUNDS: every guarded
+    global store of the step kernels checks its index and reports a miss in
+    the device error word instead of writing (see PFLBM_GUARD). Returns the
+    path of _build/checked/libpflbm.so (rebuilt when a source is newer)."""
+    lib = CHECKED / "libpflbm.so"
+    stamp = CHECKED / ".arch"
+    if (lib.exists() and stamp.exists() and stamp.read_text().strip() == platform.machine()
+            and all(p.stat().st_mtime <= lib.stat().st_mtime for p in _deps())):
+        return lib
+    CHECKED.mkdir(parents=True, exist_ok=True)
+    exe = nvcc()
+
+    def compile_one(src: str) -> Path:
+        obj = CHECKED / (Path(src).stem + ".o")
+        cmd = [exe, *ARCH, *NVCC_FLAGS, "-DPFLBM_CHECK_BOUNDS", "-c", str(CSRC / src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
+        return obj
+
+    with ThreadPoolExecutor(max_workers=jobs or min(len(SOURCES), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = lib.with_suffix(".so.tmp")
+    r = subprocess.run([exe, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, lib)
+    stamp.write_text(platform.machine())
+    return lib
+
+
 if __name__ == "__main__":
     print(build(verbose=True, force=True))

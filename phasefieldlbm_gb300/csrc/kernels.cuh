@@ -152,16 +152,22 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
             return q * N + base + o;
         };
         // collision + streaming (src/lbm.cu:172-207)
-        Store<S>::store(b.f_dst, base, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
+        const uint64_t QN = uint64_t(QQ) * N;
+        if (PFLBM_GUARD(base < N, b.err))
+            Store<S>::store(b.f_dst, base, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
 #pragma unroll
         for (int q = 1; q < QQ; q += 2) {
             T a, c;
             collide_pair<QQ, T>(q, k, a, c);
-            Store<S>::store(b.f_dst, dst_index(q), a, static_cast<T>(1.0 / weight<QQ>(q)));
-            Store<S>::store(b.f_dst, dst_index(q + 1), c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
+            const uint64_t iq = dst_index(q), iqb = dst_index(q + 1);
+            if (PFLBM_GUARD(iq < QN && iq >= q * N, b.err))
+                Store<S>::store(b.f_dst, iq, a, static_cast<T>(1.0 / weight<QQ>(q)));
+            if (PFLBM_GUARD(iqb < QN && iqb >= (q + 1) * N, b.err))
+                Store<S>::store(b.f_dst, iqb, c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
         }
         // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J)
         const T sharp = p.gamma * phi * (T(1) - phi);
+        if (!PFLBM_GUARD(base < N, b.err)) return;
         b.jflux[base] = T(4) * phi * m.ux + sharp * n_x;
         b.jflux[N + base] = T(4) * phi * m.uy + sharp * n_y;
         b.jflux[2 * N + base] = T(4) * phi * m.uz + sharp * n_z;
@@ -170,6 +176,7 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
             if (z == nz - 2) {
                 // moments of the last fluid plane for the outflow rebuild
                 const uint64_t c2 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
+                if (!PFLBM_GUARD(c2 < plane, b.err)) return;
                 T *tp = b.top;
                 tp[0 * plane + c2] = m.rho;
                 tp[1 * plane + c2] = m.ux;
@@ -188,6 +195,7 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
             if (z == 1) {
                 // moments of the first fluid plane for the inflow rebuild
                 const uint64_t c2 = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * y;
+                if (!PFLBM_GUARD(c2 < plane, b.err)) return;
                 T *bp = b.top + 13 * plane;
                 bp[0 * plane + c2] = m.ux;
                 bp[1 * plane + c2] = m.uy;
@@ -205,6 +213,7 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
             const T tf = static_cast<T>(t + 1u);
             T *av = b.avg;
             auto upd = [&](int slot, uint64_t i, T nv_) {
+                if (!PFLBM_GUARD(i < N, b.err)) return;
                 const T o = av[slot * N + i];
                 av[slot * N + i] = o + (nv_ - o) / tf;
             };

@@ -94,6 +94,17 @@ struct StepBuffers {
     const float *mlp;  // closure network blob (MODE_STEP_CLOSURE)
 };
 
+// Index guard of the step kernels' global stores. Built with
+// -DPFLBM_CHECK_BOUNDS (a test build), every guarded store first checks its
+// index against the array's extent and, when outside, sets bit 4 of the
+// device error word and skips the store; otherwise the guard is `true` and
+// costs nothing.
+#ifdef PFLBM_CHECK_BOUNDS
+#define PFLBM_GUARD(in_range, err) ((in_range) ? true : (atomicOr((err), 4u), false))
+#else
+#define PFLBM_GUARD(in_range, err) true
+#endif
+
 // Order of the macroscopic arrays in the analysis cache; equals
 // pflbm_field_id 0..17.
 enum MacroSlot { M_RHO = 0, M_UX, M_UY, M_UZ, M_PXX, M_PYY, M_PZZ, M_PXY, M_PXZ, M_PYZ,

@@ -64,7 +64,7 @@ __device__ __forceinline__ void phase_node(const Params<typename Store<S>::T> &p
     }
     T s = T(0);
     s += g0; s += g1; s += g2; s += g3; s += g4; s += g5; s += g6;
-    b.phi_dst[X] = s;
+    if (PFLBM_GUARD(X < N, b.err)) b.phi_dst[X] = s;
 
     if constexpr (JET) {
         if (z == 1) {
@@ -88,6 +88,7 @@ __device__ __forceinline__ void phase_node(const Params<typename Store<S>::T> &p
                         T bux, buy, buz;
                         inflow_velocity<T>(p, gx, gy, t, bux, buy, buz);
                         const T v = feq_q<QQ, T>(q, T(1), bux, buy, buz) + p.omco_zmin * fneq_q<QQ, T>(q, kX);
+                        if (PFLBM_GUARD(static_cast<uint64_t>(gx) + static_cast<uint64_t>(nx) * gy < plane, b.err))
                         Store<S>::store(b.f_dst, q * N + static_cast<uint64_t>(gx) + static_cast<uint64_t>(nx) * gy, v,
                                         static_cast<T>(1.0 / weight<QQ>(q)));
                     }
@@ -97,7 +98,7 @@ __device__ __forceinline__ void phase_node(const Params<typename Store<S>::T> &p
         if (z == nz - 2) {
             // ghost phi of the outlet plane takes this step's value
             // (BoundaryConditions.cuh:127)
-            b.phi_dst[idx(x, y, nz - 1)] = phiX;
+            if (PFLBM_GUARD(idx(x, y, nz - 1) < N, b.err)) b.phi_dst[idx(x, y, nz - 1)] = phiX;
             // outflow rebuild of the populations entering (x,y,nz-2) from
             // the ghost plane: equilibrium of the in-plane source column
             // (x-cx, y-cy), non-equilibrium and force of this node.
@@ -123,7 +124,8 @@ __device__ __forceinline__ void phase_node(const Params<typename Store<S>::T> &p
                                 T(0.5) * force_q<QQ, T>(q, uxb, uyb, uzb, fxX, fyX, fzX);
                     const uint64_t dst = q * N + static_cast<uint64_t>(x - kCX[q]) +
                                          static_cast<uint64_t>(nx) * (static_cast<uint64_t>(y - kCY[q]) + static_cast<uint64_t>(ny) * (nz - 1));
-                    Store<S>::store(b.f_dst, dst, v, static_cast<T>(1.0 / weight<QQ>(q)));
+                    if (PFLBM_GUARD(dst < uint64_t(QQ) * N, b.err))
+                        Store<S>::store(b.f_dst, dst, v, static_cast<T>(1.0 / weight<QQ>(q)));
                 }
             }
         }
@@ -207,6 +209,7 @@ __device__ __forceinline__ void phase_vec4(const Params<float> &p, const StepBuf
         out[k] = s;
     }
     // ghost columns keep their (zero) phi; write only interior nodes
+    if (!PFLBM_GUARD(r0 + x4 + 3 < N, b.err)) return;
     if (x4 >= 1 && x4 + 3 <= nx - 2) {
         *reinterpret_cast<float4 *>(b.phi_dst + r0 + x4) = make_float4(out[0], out[1], out[2], out[3]);
     } else {
