@@ -282,8 +282,26 @@ def run_gpu(args, ranks: Ranks) -> dict:
     sim.close()
 
     # other lattices / storage precisions on the same jet (informational)
+    # other lattices / storage precisions on the same jet, each with its error
+    # against the FP64 path after the same number of steps (rel. L2 of rho,
+    # the centreline u_z and phi)
     variants = {}
     if not args.no_variants:
+        vsteps = 3 * inner // 2 + 2 * inner
+        fp64_ref = {}
+
+        def errors(wl, s2):
+            if wl not in fp64_ref:
+                with pf.Simulation(pf.preset(wl, storage=pf.STORAGE_FP64, device=cfg.device)) as s64:
+                    s64.step(vsteps)
+                    fp64_ref[wl] = {f: s64.get_field(f, dtype=np.float64) for f in ("rho", "uz", "phi")}
+            ref = fp64_ref[wl]
+            cy, cx = ref["uz"].shape[1] // 2, ref["uz"].shape[2] // 2
+            got = {f: s2.get_field(f, dtype=np.float64) for f in ("rho", "uz", "phi")}
+            rl2 = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            return {"rho": rl2(got["rho"], ref["rho"]), "uz_centreline": rl2(got["uz"][:, cy, cx], ref["uz"][:, cy, cx]),
+                    "phi": rl2(got["phi"], ref["phi"])}
+
         for name, wl, st in (("jet_d3q19_fp32", "jet_d3q19", pf.STORAGE_FP32),
                              ("jet_d3q19_fp16", "jet_d3q19", pf.STORAGE_FP16),
                              ("jet_d3q19_bf16", "jet_d3q19", pf.STORAGE_BF16),
@@ -294,7 +312,8 @@ def run_gpu(args, ranks: Ranks) -> dict:
                 s2.synchronize()
                 tot2, k2 = s2.step_profiled(2 * inner)
                 variants[name] = {"mlups": round(c2.nodes * 2 * inner / (tot2 / 1e3) / 1e6, 1),
-                                  "collide_ms": round(k2[0] / (2 * inner), 4), "phase_ms": round(k2[1] / (2 * inner), 4)}
+                                  "collide_ms": round(k2[0] / (2 * inner), 4), "phase_ms": round(k2[1] / (2 * inner), 4),
+                                  "steps": vsteps, "rel_l2_vs_fp64": errors(wl, s2)}
 
     cpu = None
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
