@@ -160,6 +160,10 @@ int validate(const pflbm_config &c) {
         return fail(PFLBM_ERR_INVALID_ARG, "storage must be FP32, FP16, BF16 or FP64");
     if (c.nx < 5 || c.ny < 5 || c.nz < 5) return fail(PFLBM_ERR_INVALID_ARG, "nx, ny, nz must be >= 5");
     if (c.nx > 65536 || c.ny > 65536 || c.nz > 65536) return fail(PFLBM_ERR_INVALID_ARG, "dimension above 65536");
+    // the step kernels index a node within one array with 32 bits (a grid
+    // this large would not fit in device memory anyway)
+    if (uint64_t(c.nx) * c.ny * c.nz >= (uint64_t(1) << 32))
+        return fail(PFLBM_ERR_INVALID_ARG, "grid of 2^32 nodes or more");
     if (!(c.interface_width > 0.0f)) return fail(PFLBM_ERR_INVALID_ARG, "interface_width must be > 0");
     if (c.inflow_noise != PFLBM_NOISE_GAUSSIAN_UXY && c.inflow_noise != PFLBM_NOISE_UNIFORM_UZ)
         return fail(PFLBM_ERR_INVALID_ARG, "inflow_noise must be 0 or 1");

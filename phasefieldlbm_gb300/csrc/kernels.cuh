@@ -75,7 +75,9 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
     using T = typename Store<S>::T;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N, plane = p.plane;
-    const uint64_t base = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * (y + static_cast<uint64_t>(ny) * z);
+    // node index, 32-bit (N < 2^32 is checked on the host)
+    const uint32_t node = uint32_t(x) + uint32_t(nx) * (uint32_t(y) + uint32_t(ny) * uint32_t(z));
+    const uint64_t base = node;
     const T st = -p.sigma * curvature * ind;
     const T fx = st * n_x, fy = st * n_y, fz = st * n_z;
 
@@ -131,39 +133,42 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
         mc[M_FZ * N + base] = fz;
         return;
     } else {
-        // periodic-edge store offsets: P = wrap(S + c) - c
-        const int64_t ex_p = (x == nx - 2) ? -(int64_t)(nx - 2) : 0;  // cx = +1
-        const int64_t ex_m = (x == 1) ? (int64_t)(nx - 2) : 0;        // cx = -1
-        const int64_t ey_p = (y == ny - 2) ? -(int64_t)(ny - 2) * nx : 0;
-        const int64_t ey_m = (y == 1) ? (int64_t)(ny - 2) * nx : 0;
-        int64_t ez_p = 0, ez_m = 0;
+        // periodic-edge store offsets: P = wrap(S + c) - c. Node indices
+        // within one direction's array are 32-bit (N < 2^32 is checked on
+        // the host); negative offsets are two's-complement and the sum wraps
+        // back into [0, N) exactly.
+        const uint32_t ex_p = (x == nx - 2) ? 0u - uint32_t(nx - 2) : 0u;  // cx = +1
+        const uint32_t ex_m = (x == 1) ? uint32_t(nx - 2) : 0u;            // cx = -1
+        const uint32_t ey_p = (y == ny - 2) ? 0u - uint32_t(ny - 2) * uint32_t(nx) : 0u;
+        const uint32_t ey_m = (y == 1) ? uint32_t(ny - 2) * uint32_t(nx) : 0u;
+        uint32_t ez_p = 0u, ez_m = 0u;
         if constexpr (!JET) {
-            ez_p = (z == nz - 2) ? -(int64_t)(nz - 2) * (int64_t)plane : 0;
-            ez_m = (z == 1) ? (int64_t)(nz - 2) * (int64_t)plane : 0;
+            ez_p = (z == nz - 2) ? 0u - uint32_t(nz - 2) * uint32_t(plane) : 0u;
+            ez_m = (z == 1) ? uint32_t(nz - 2) * uint32_t(plane) : 0u;
         }
-        auto dst_index = [&](int q) -> uint64_t {
-            int64_t o = 0;
+        auto dst_node = [&](int q) -> uint32_t {
+            uint32_t o = node;
             if (kCX[q] > 0) o += ex_p;
             if (kCX[q] < 0) o += ex_m;
             if (kCY[q] > 0) o += ey_p;
             if (kCY[q] < 0) o += ey_m;
             if (kCZ[q] > 0) o += ez_p;
             if (kCZ[q] < 0) o += ez_m;
-            return q * N + base + o;
+            return o;
         };
-        // collision + streaming (src/lbm.cu:172-207)
-        const uint64_t QN = uint64_t(QQ) * N;
+        // collision + streaming (src/lbm.cu:172-207); direction q's array
+        // starts at f_dst + q N
         if (PFLBM_GUARD(base < N, b.err))
-            Store<S>::store(b.f_dst, base, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
+            Store<S>::store(b.f_dst, node, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
 #pragma unroll
         for (int q = 1; q < QQ; q += 2) {
             T a, c;
             collide_pair<QQ, T>(q, k, a, c);
-            const uint64_t iq = dst_index(q), iqb = dst_index(q + 1);
-            if (PFLBM_GUARD(iq < QN && iq >= q * N, b.err))
-                Store<S>::store(b.f_dst, iq, a, static_cast<T>(1.0 / weight<QQ>(q)));
-            if (PFLBM_GUARD(iqb < QN && iqb >= (q + 1) * N, b.err))
-                Store<S>::store(b.f_dst, iqb, c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
+            const uint32_t iq = dst_node(q), iqb = dst_node(q + 1);
+            if (PFLBM_GUARD(iq < N, b.err))
+                Store<S>::store(b.f_dst + uint64_t(q) * N, iq, a, static_cast<T>(1.0 / weight<QQ>(q)));
+            if (PFLBM_GUARD(iqb < N, b.err))
+                Store<S>::store(b.f_dst + uint64_t(q + 1) * N, iqb, c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
         }
         // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J)
         const T sharp = p.gamma * phi * (T(1) - phi);
