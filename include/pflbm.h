@@ -255,6 +255,16 @@ int pflbm_device_bytes(const pflbm_sim *sim, uint64_t *bytes);
  * 16-byte aligned rows: nx*element size % 16 == 0), 0 for plain loads. */
 int pflbm_uses_tma(const pflbm_sim *sim, int32_t *flag);
 
+/* Which collide kernel the plain time step runs (the averaging and closure
+ * steps always use one node per thread): */
+typedef enum {
+    PFLBM_COLLIDE_PLAIN = 0,     /* plain loads, one node per thread */
+    PFLBM_COLLIDE_TMA = 1,       /* TMA-fed, one node per thread */
+    PFLBM_COLLIDE_TMA_PAIRS = 2  /* TMA-fed, two x-adjacent nodes per thread with packed FP32x2 arithmetic
+                                    (16-bit storage, D3Q19) */
+} pflbm_collide_variant_t;
+int pflbm_collide_variant(const pflbm_sim *sim, int32_t *variant);
+
 /* Number of CUDA kernels one time step launches (launch accounting). */
 int pflbm_kernels_per_step(const pflbm_sim *sim, int32_t *count);
 

@@ -47,7 +47,7 @@ EXPORTED_SYMBOLS = [
     "pflbm_init", "pflbm_set_initial_field", "pflbm_step", "pflbm_step_async",
     "pflbm_synchronize", "pflbm_step_profiled", "pflbm_current_step", "pflbm_get_field", "pflbm_get_field_f64",
     "pflbm_reduce", "pflbm_write_output", "pflbm_save_checkpoint", "pflbm_load_checkpoint",
-    "pflbm_device_bytes", "pflbm_uses_tma", "pflbm_kernels_per_step",
+    "pflbm_device_bytes", "pflbm_uses_tma", "pflbm_collide_variant", "pflbm_kernels_per_step",
     "pflbm_destroy",
     "pflbm_ensemble_create", "pflbm_ensemble_init", "pflbm_ensemble_step", "pflbm_ensemble_step_profiled",
     "pflbm_ensemble_get_field", "pflbm_ensemble_reduce", "pflbm_ensemble_set_tuning", "pflbm_ensemble_autotune",
@@ -168,6 +168,7 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_load_checkpoint": ([vp, ctypes.c_char_p], ctypes.c_int),
         "pflbm_kernels_per_step": ([vp, ctypes.POINTER(i32)], ctypes.c_int),
         "pflbm_uses_tma": ([vp, ctypes.POINTER(i32)], ctypes.c_int),
+        "pflbm_collide_variant": ([vp, ctypes.POINTER(i32)], ctypes.c_int),
         "pflbm_destroy": ([vp], ctypes.c_int),
         "pflbm_ensemble_create": ([ctypes.POINTER(Config), i32, ctypes.POINTER(vp)], ctypes.c_int),
         "pflbm_ensemble_init": ([vp], ctypes.c_int),
@@ -477,6 +478,13 @@ class Simulation:
         v = ctypes.c_int32()
         _check(self.lib, self.lib.pflbm_uses_tma(self._h, ctypes.byref(v)))
         return bool(v.value)
+
+    @property
+    def collide_variant(self) -> str:
+        """Collide kernel of the plain step: "plain", "tma" or "tma_pairs"."""
+        v = ctypes.c_int32()
+        _check(self.lib, self.lib.pflbm_collide_variant(self._h, ctypes.byref(v)))
+        return ("plain", "tma", "tma_pairs")[v.value]
 
     @property
     def kernels_per_step(self) -> int:

@@ -933,6 +933,12 @@ int pflbm_uses_tma(const pflbm_sim *s, int32_t *flag) {
     return PFLBM_OK;
 }
 
+int pflbm_collide_variant(const pflbm_sim *s, int32_t *variant) {
+    if (!s || !variant) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
+    *variant = s->eng->collide_variant();
+    return PFLBM_OK;
+}
+
 int pflbm_kernels_per_step(const pflbm_sim *s, int32_t *count) {
     if (!s || !count) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
     *count = s->eng->kernels_per_step();

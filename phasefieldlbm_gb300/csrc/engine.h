@@ -68,6 +68,7 @@ class Engine {
     virtual unsigned int *error_word() = 0;
     // True when the TMA-fed collide kernel is in use.
     virtual bool uses_tma() const = 0;
+    virtual int collide_variant() const = 0;  // pflbm_collide_variant_t
     virtual int kernels_per_step() const = 0;
     // Learned closure: copies the network blob (kMlpBlob floats, host) to the
     // device and switches the collide kernel to the closure mode; null

@@ -10,6 +10,7 @@
 
 #include "engine.h"
 #include "kernels.cuh"
+#include "kernels_pair.cuh"
 #include "kernels_tma.cuh"
 
 namespace pflbm {
@@ -187,6 +188,24 @@ class EngineT final : public Engine {
             return;
         }
         use_tma_ = true;
+        // two nodes per thread with packed FP32x2 arithmetic for the plain
+        // step of 16-bit D3Q19 storage, whose collide is issue-bound (FP32
+        // and D3Q27 stay faster with one node per thread and twice the
+        // warps). PFLBM_NO_PAIR=1 keeps one node per thread; PFLBM_PAIR=1
+        // selects the pair kernel for every FP32/16-bit lattice (tests).
+        use_pair_ = false;
+        if constexpr (sizeof(T) == 4) {
+            const char *no = std::getenv("PFLBM_NO_PAIR");
+            const char *force = std::getenv("PFLBM_PAIR");
+            const bool want = (force && force[0] == '1') || (sizeof(S) == 2 && QQ == 19);
+            if (want && !(no && no[0] == '1') && h_.nx % 2 == 0) {
+                if (cudaFuncSetAttribute(k_collide_pair<QQ, JET, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(PairLayout<QQ, S>::total)) == cudaSuccess)
+                    use_pair_ = true;
+                else
+                    cudaGetLastError();
+            }
+        }
     }
 
     void free_all() override {
@@ -243,12 +262,17 @@ class EngineT final : public Engine {
             }
         } else if (use_tma_) {
             const size_t sm = TmaLayout<QQ, S>::total;
-            if (avg_)
+            if (avg_) {
                 k_collide_tma<QQ, JET, S, MODE_STEP_AVG>
                     <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmap_[parity], phimap_[parity]);
-            else
+            } else if (use_pair_) {
+                if constexpr (sizeof(T) == 4)
+                    k_collide_pair<QQ, JET, S><<<collide_grid(), dim3(TX2, TY, 1), PairLayout<QQ, S>::total, s>>>(
+                        p_, b, fmap_[parity], phimap_[parity]);
+            } else {
                 k_collide_tma<QQ, JET, S, MODE_STEP>
                     <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+            }
         } else if (avg_) {
             k_collide<QQ, JET, S, MODE_STEP_AVG><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
         } else {
@@ -320,6 +344,7 @@ class EngineT final : public Engine {
         cudaStreamSynchronize(s);
     }
     bool uses_tma() const override { return use_tma_; }
+    int collide_variant() const override { return use_pair_ ? 2 : (use_tma_ ? 1 : 0); }
     int real_bytes() const override { return int(sizeof(T)); }
     void *macro_ptr() override { return macro_; }
     void *avg_ptr() override { return avg_; }
@@ -365,6 +390,7 @@ class EngineT final : public Engine {
     double *partial_ = nullptr;
     unsigned int *err_ = nullptr;
     bool use_tma_ = false;
+    bool use_pair_ = false;  // k_collide_pair for the plain step
     bool no_vec_ = false;  // PFLBM_NO_VEC=1: scalar phase kernel
     float *mlp_ = nullptr;  // closure network blob (kMlpBlob floats)
     bool closure_ = false;

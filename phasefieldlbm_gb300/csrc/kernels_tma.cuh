@@ -51,9 +51,13 @@ struct TmaPlan {
     static constexpr size_t phi_slot_bytes = align128(phi_plane_bytes);
     static constexpr size_t off_f = 0;
     static constexpr size_t off_phi = align128(NS * stage_bytes);
+    // n^ (3 components) of 4 planes on the tile + halo 1
     static constexpr size_t off_n = align128(off_phi + kPhiSlots * phi_slot_bytes);
-    static constexpr size_t n_bytes = size_t(4) * 4 * NY_ * NX_ * sizeof(T);
-    static constexpr size_t off_bar = align128(off_n + n_bytes);
+    static constexpr size_t n_bytes = size_t(3) * 4 * NY_ * NX_ * sizeof(T);
+    // |grad phi| of 3 planes, tile rows only (rows of the halo width)
+    static constexpr size_t off_ind = align128(off_n + n_bytes);
+    static constexpr size_t ind_bytes = size_t(3) * TY * NX_ * sizeof(T);
+    static constexpr size_t off_bar = align128(off_ind + ind_bytes);
     static constexpr size_t total = off_bar + 128;  // NS mbarriers + the abort flag
     static constexpr uint32_t tx_bytes = uint32_t(QQ * box_bytes + phi_plane_bytes);
     static_assert(box_stride % 128 == 0 && phi_slot_bytes % 128 == 0 && off_phi % 128 == 0, "TMA smem alignment");
@@ -92,9 +96,8 @@ template <int QQ, class S>
 using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S>::value>;
 
 // Barriers of the TMA pipeline: once per CTA, before its first tile.
-template <int QQ, class S>
+template <int QQ, class S, class L = TmaLayout<QQ, S>>
 __device__ __forceinline__ void tma_pipeline_init(unsigned char *smem) {
-    using L = TmaLayout<QQ, S>;
     if (threadIdx.x + blockDim.x * threadIdx.y == 0) {
         uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
         for (int k = 0; k < L::kStages; ++k) mbar_init(&bar[k], 1);
@@ -119,6 +122,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
     S *s_f = reinterpret_cast<S *>(smem + L::off_f);
     T *s_phi = reinterpret_cast<T *>(smem + L::off_phi);
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);
+    T *s_ind = reinterpret_cast<T *>(smem + L::off_ind);
     constexpr int NS = L::kStages, R = L::kPhiSlots;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
     volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L::off_bar + 8 * NS);
@@ -135,6 +139,8 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
                                       (size_t(ly) * L::PBW + lx) * sizeof(T));
     };
     auto n_at = [&](int c, int slot, int ly, int lx) -> T & { return s_n[((c * 4 + slot) * NY_ + ly) * NX_ + lx]; };
+    // |grad phi| of plane zp at tile row r, halo column lx (slot zp % 3)
+    auto ind_at = [&](int zp, int r, int lx) -> T & { return s_ind[((zp % 3) * TY + r) * NX_ + lx]; };
     auto issue = [&](int stage, int zf) {
         // generic-proxy accesses to the recycled slots are ordered before the
         // async-proxy writes by the preceding block barrier and this fence
@@ -189,7 +195,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
             n_at(0, nn, ly, lx) = nxv;
             n_at(1, nn, ly, lx) = nyv;
             n_at(2, nn, ly, lx) = nzv;
-            n_at(3, nn, ly, lx) = ind;
+            if (ly >= 1 && ly <= TY) ind_at(zp, ly - 1, lx) = ind;
         }
     };
     __syncthreads();
@@ -229,7 +235,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         const T scy = lattice_grad<QQ, 1, T>([&](int dx, int dy, int dz) { return nv(1, dx, dy, dz); });
         const T scz = lattice_grad<QQ, 2, T>([&](int dx, int dy, int dz) { return nv(2, dx, dy, dz); });
         const T curvature = T(3) * (scx + scy + scz);
-        const T n_x = nv(0, 0, 0, 0), n_y = nv(1, 0, 0, 0), n_z = nv(2, 0, 0, 0), ind = nv(3, 0, 0, 0);
+        const T n_x = nv(0, 0, 0, 0), n_y = nv(1, 0, 0, 0), n_z = nv(2, 0, 0, 0), ind = ind_at(z, ty, tx + 1);
         const T phi = phi_at(pslot(z), ty + 2, tx + L::PXO);
 
         T pop[QQ];

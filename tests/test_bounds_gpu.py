@@ -23,7 +23,9 @@ def _cases(pf):
                   flags=pf.FLAG_TIME_AVERAGE | pf.FLAG_REYNOLDS_MOMENTS)
     out.append(("jet27_fp16_avg", c))
     c = pf.preset("jet_d3q19", nx=64, ny=64, nz=96, diam=12, radius=6, storage=pf.STORAGE_BF16)
-    out.append(("jet19_bf16", c))
+    out.append(("jet19_bf16_pairs", c))                              # node-pair collide
+    c = pf.preset("jet_d3q19", nx=72, ny=40, nz=48, diam=10, radius=5, storage=pf.STORAGE_FP16)
+    out.append(("jet19_fp16_pairs_overhang", c))                     # node pairs, last tile past the grid
     c = pf.config_reference(pf.CASE_DROPLET, pf.VS_D3Q27)
     c.nx = c.ny = c.nz = 48
     c.radius, c.diam = 12, 24

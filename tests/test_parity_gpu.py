@@ -209,25 +209,83 @@ def test_tma_and_vector_paths_bit_identical(pflbm, monkeypatch, vs, storage, avg
     # The TMA-fed collide kernel and the float4 phase kernel compute exactly
     # what the plain-load kernels compute; only the data movement differs
     # (avg: the collide mode that also updates the time averages).
+    # (one node per thread: the node-pair kernel is compared below)
     c = jet_cfg(pflbm, vs, nx=64, ny=40, nz=48, diam=10, noise=1)
     c.storage = storage
     if avg:
         c.flags = pflbm.FLAG_TIME_AVERAGE | pflbm.FLAG_REYNOLDS_MOMENTS
     fields = ALL18 + (AVG_FIELDS if avg else ())
     out = {}
+    monkeypatch.setenv("PFLBM_NO_PAIR", "1")
     for mode in ("fast", "plain"):
         if mode == "plain":
             monkeypatch.setenv("PFLBM_NO_TMA", "1")
             monkeypatch.setenv("PFLBM_NO_VEC", "1")
         with pflbm.Simulation(c) as s:
             if mode == "fast":
-                assert s.uses_tma
+                assert s.uses_tma and s.collide_variant == "tma"
             else:
-                assert not s.uses_tma
+                assert not s.uses_tma and s.collide_variant == "plain"
             s.step(33)
             out[mode] = {f: s.get_field(f, dtype=np.float64) for f in fields}
     for f in fields:
         assert np.array_equal(out["fast"][f], out["plain"][f]), f
+
+
+PAIR_TOL = {  # rel. L2 of the node-pair kernel against the one-node kernel: rho, phi, u
+    0: (1e-6, 1e-6, 3e-5),    # FP32: rounding of the reordered algebra
+    1: (1e-5, 5e-5, 2e-3),    # FP16: the last stored bit differs now and then
+    2: (5e-5, 5e-4, 1e-2),    # BF16
+}
+
+
+@pytest.mark.parametrize("case,vs,storage", [
+    ("jet", 19, 1), ("droplet", 19, 1), ("jet", 19, 2), ("jet_overhang", 19, 1),
+    ("jet", 19, 0), ("droplet", 19, 0), ("jet", 27, 0), ("droplet", 27, 0), ("jet", 27, 1),
+])
+def test_pair_kernel_matches_one_node_kernel(pflbm, monkeypatch, case, vs, storage):
+    # The node-pair collide (two x-adjacent nodes per thread, packed FP32x2
+    # arithmetic, default for 16-bit D3Q19) against the one-node TMA kernel.
+    # FP32 and D3Q27 run it only when PFLBM_PAIR=1 selects it; the FP32
+    # cases pin its algebra at FP32 rounding. jet_overhang: nx = 72, the
+    # last column tile extends past the grid.
+    if case == "droplet":
+        c = droplet_cfg(pflbm, vs, n=48, radius=10)
+        steps = 60
+    elif case == "jet_overhang":
+        c = jet_cfg(pflbm, vs, nx=72, ny=36, nz=40, diam=8, noise=1)
+        steps = 25
+    else:
+        c = jet_cfg(pflbm, vs, nx=64, ny=40, nz=48, diam=10, noise=1)
+        steps = 33
+    c.storage = storage
+    out = {}
+    for mode in ("pair", "one"):
+        if mode == "pair":
+            monkeypatch.setenv("PFLBM_PAIR", "1")
+        else:
+            monkeypatch.delenv("PFLBM_PAIR", raising=False)
+            monkeypatch.setenv("PFLBM_NO_PAIR", "1")
+        with pflbm.Simulation(c) as s:
+            assert s.collide_variant == ("tma_pairs" if mode == "pair" else "tma")
+            s.step(steps)
+            out[mode] = {f: s.get_field(f, dtype=np.float64) for f in BASIC}
+    t_rho, t_phi, t_u = PAIR_TOL[storage]
+    e = {f: rel_l2(out["pair"][f], out["one"][f]) for f in BASIC}
+    e["u"] = rel_l2(np.stack([out["pair"][f] for f in ("ux", "uy", "uz")]),
+                    np.stack([out["one"][f] for f in ("ux", "uy", "uz")]))
+    assert e["rho"] <= t_rho and e["phi"] <= t_phi and e["u"] <= t_u, e
+
+
+def test_pair_kernel_is_the_default_for_16bit_d3q19(pflbm, monkeypatch):
+    monkeypatch.delenv("PFLBM_PAIR", raising=False)
+    monkeypatch.delenv("PFLBM_NO_PAIR", raising=False)
+    for vs, storage, want in ((19, 1, "tma_pairs"), (19, 2, "tma_pairs"), (19, 0, "tma"), (27, 1, "tma"),
+                              (27, 0, "tma"), (19, 3, "tma")):
+        c = jet_cfg(pflbm, vs, nx=64, ny=40, nz=48, diam=10)
+        c.storage = storage
+        with pflbm.Simulation(c) as s:
+            assert s.collide_variant == want, (vs, storage)
 
 
 @pytest.mark.parametrize("storage", [0, 1])
