@@ -13,9 +13,12 @@
 // Interior node pairs store each direction as one 8-byte (FP32) or 4-byte
 // (16-bit) word. The two pairs at the periodic x edges, where one node of the
 // pair is a ghost, store the active node alone with its wrap offsets. With
-// 16-bit storage the collision is evaluated directly in the scaled unknown
-// f'/w_q, so no per-direction rescaling precedes the conversion, and the
-// three reciprocals of a node use the approximate hardware reciprocal.
+// 16-bit storage the three reciprocals of a node use the approximate hardware
+// reciprocal. (Evaluating the collision directly in the stored unknown f'/w_q
+// saves the rescaling multiply but was measurably less accurate against the
+// FP64 path: rho 2.6x, u_z 1.4x the error of the one-node kernel after 400
+// jet steps. The exact scaled values round to 16 bits coherently, where the
+// unscaled form's FP32 rounding dithers them.)
 //
 // Used for the plain step (no time averages, no closure) with FP32, FP16 or
 // BF16 storage; the TMA row alignment already makes nx even.
@@ -80,40 +83,44 @@ template <class S>
 struct PairStore;
 template <>
 struct PairStore<float> {
-    static constexpr bool kScaled = false;
+    static constexpr bool kScaled = false;  // stores f'
     template <bool ALIGNED>
     static __device__ __forceinline__ V2 load(const float *p) {
         if constexpr (ALIGNED) return V2(*reinterpret_cast<const float2 *>(p));
         else return V2(p[0], p[1]);
     }
-    static __device__ __forceinline__ void store2(float *p, V2 v) { *reinterpret_cast<float2 *>(p) = v.v; }
-    static __device__ __forceinline__ void store1(float *p, float v) { *p = v; }
+    static __device__ __forceinline__ void store2(float *p, V2 v, float) { *reinterpret_cast<float2 *>(p) = v.v; }
+    static __device__ __forceinline__ void store1(float *p, float v, float) { *p = v; }
 };
 template <>
 struct PairStore<__half> {
-    static constexpr bool kScaled = true;
+    static constexpr bool kScaled = true;  // stores f'/w_q
     template <bool ALIGNED>
     static __device__ __forceinline__ V2 load(const __half *p) {
         if constexpr (ALIGNED) return V2(__half22float2(*reinterpret_cast<const __half2 *>(p)));
         else return V2(__half2float(p[0]), __half2float(p[1]));
     }
-    static __device__ __forceinline__ void store2(__half *p, V2 v) {
-        *reinterpret_cast<__half2 *>(p) = __floats2half2_rn(v.v.x, v.v.y);
+    static __device__ __forceinline__ void store2(__half *p, V2 v, float inv_w) {
+        const V2 s = v * V2(inv_w);
+        *reinterpret_cast<__half2 *>(p) = __floats2half2_rn(s.v.x, s.v.y);
     }
-    static __device__ __forceinline__ void store1(__half *p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ void store1(__half *p, float v, float inv_w) { *p = __float2half_rn(v * inv_w); }
 };
 template <>
 struct PairStore<__nv_bfloat16> {
-    static constexpr bool kScaled = true;
+    static constexpr bool kScaled = true;  // stores f'/w_q
     template <bool ALIGNED>
     static __device__ __forceinline__ V2 load(const __nv_bfloat16 *p) {
         if constexpr (ALIGNED) return V2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(p)));
         else return V2(__bfloat162float(p[0]), __bfloat162float(p[1]));
     }
-    static __device__ __forceinline__ void store2(__nv_bfloat16 *p, V2 v) {
-        *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(v.v.x, v.v.y);
+    static __device__ __forceinline__ void store2(__nv_bfloat16 *p, V2 v, float inv_w) {
+        const V2 s = v * V2(inv_w);
+        *reinterpret_cast<__nv_bfloat162 *>(p) = __floats2bfloat162_rn(s.v.x, s.v.y);
     }
-    static __device__ __forceinline__ void store1(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void store1(__nv_bfloat16 *p, float v, float inv_w) {
+        *p = __float2bfloat16_rn(v * inv_w);
+    }
 };
 
 // ------------------------------------------------------- per-pair algebra
@@ -187,22 +194,21 @@ __device__ __forceinline__ Macro2 moments2(const V2 (&f)[QQ], V2 fx, V2 fy, V2 f
     return m;
 }
 
-// CollideCtx of lattice.cuh on node pairs. SCALED: the outputs are f'/w_q,
-// which makes every weight-class factor the same (w_q divides out).
-template <int QQ, bool SCALED>
+// CollideCtx of lattice.cuh on node pairs.
+template <int QQ>
 struct Ctx2 {
     V2 fx, fy, fz;
     V2 pxx, pyy, pzz, pxy, pxz, pyz;
     V2 dxy, dxz, dyz;  // pxx + pyy, pxx + pzz, pyy + pzz
     V2 A, nuF;         // 1 - 1.5 |u|^2, -u.F
     V2 u3x, u3y, u3z;  // 3 u
-    V2 wr[4], ow[4];   // w_c rho, (1 - omega) 4.5 w_c (SCALED: rho, (1 - omega) 4.5 in [0])
+    V2 wr[4], ow[4];   // w_c rho, (1 - omega) 4.5 w_c
     V2 h1, h2, h3, h4, h5, h6, h7;
 };
 
-template <int QQ, bool SCALED>
-__device__ __forceinline__ Ctx2<QQ, SCALED> make_ctx2(const Macro2 &m, V2 fx, V2 fy, V2 fz, V2 omco) {
-    Ctx2<QQ, SCALED> k;
+template <int QQ>
+__device__ __forceinline__ Ctx2<QQ> make_ctx2(const Macro2 &m, V2 fx, V2 fy, V2 fz, V2 omco) {
+    Ctx2<QQ> k;
     k.fx = fx; k.fy = fy; k.fz = fz;
     k.pxx = m.pxx; k.pyy = m.pyy; k.pzz = m.pzz; k.pxy = m.pxy; k.pxz = m.pxz; k.pyz = m.pyz;
     k.dxy = m.pxx + m.pyy;
@@ -213,16 +219,11 @@ __device__ __forceinline__ Ctx2<QQ, SCALED> make_ctx2(const Macro2 &m, V2 fx, V2
     k.u3x = V2(3.0f) * m.ux;
     k.u3y = V2(3.0f) * m.uy;
     k.u3z = V2(3.0f) * m.uz;
-    if constexpr (SCALED) {
-        k.wr[0] = m.rho;
-        k.ow[0] = omco * V2(4.5f);
-    } else {
-        const double wc[4] = {Weights<QQ>::w0, Weights<QQ>::w1, Weights<QQ>::w2, Weights<QQ>::w3};
+    const double wc[4] = {Weights<QQ>::w0, Weights<QQ>::w1, Weights<QQ>::w2, Weights<QQ>::w3};
 #pragma unroll
-        for (int c = 0; c < (QQ == 27 ? 4 : 3); ++c) {
-            k.wr[c] = V2(static_cast<float>(wc[c])) * m.rho;
-            k.ow[c] = omco * V2(static_cast<float>(4.5 * wc[c]));
-        }
+    for (int c = 0; c < (QQ == 27 ? 4 : 3); ++c) {
+        k.wr[c] = V2(static_cast<float>(wc[c])) * m.rho;
+        k.ow[c] = omco * V2(static_cast<float>(4.5 * wc[c]));
     }
     if constexpr (QQ == 27) {
         const V2 two(2.0f);
@@ -248,8 +249,8 @@ __device__ __forceinline__ V2 cdot2(int cx, int cy, int cz, V2 vx, V2 vy, V2 vz)
 }
 
 // c . Pi . c for the trace-free Pi.
-template <int QQ, bool SCALED>
-__device__ __forceinline__ V2 cpic2(int cx, int cy, int cz, const Ctx2<QQ, SCALED> &k) {
+template <int QQ>
+__device__ __forceinline__ V2 cpic2(int cx, int cy, int cz, const Ctx2<QQ> &k) {
     const int nnz = (cx != 0) + (cy != 0) + (cz != 0);
     if (nnz == 1) return cx != 0 ? k.pxx : (cy != 0 ? k.pyy : k.pzz);
     if (nnz == 2) {
@@ -261,8 +262,8 @@ __device__ __forceinline__ V2 cpic2(int cx, int cy, int cz, const Ctx2<QQ, SCALE
 }
 
 // 3 x the third-order Hermite part (D3Q27), odd in c.
-template <int QQ, bool SCALED>
-__device__ __forceinline__ V2 hermite3_2(int cx, int cy, int cz, const Ctx2<QQ, SCALED> &k) {
+template <int QQ>
+__device__ __forceinline__ V2 hermite3_2(int cx, int cy, int cz, const Ctx2<QQ> &k) {
     const int a[7] = {cy * (3 * cx * cx - 1), cz * (3 * cx * cx - 1), cx * (3 * cy * cy - 1), cz * (3 * cy * cy - 1),
                       cx * (3 * cz * cz - 1), cy * (3 * cz * cz - 1), cx * cy * cz};
     const V2 h[7] = {k.h1, k.h2, k.h3, k.h4, k.h5, k.h6, k.h7};
@@ -283,24 +284,24 @@ __device__ __forceinline__ V2 hermite3_2(int cx, int cy, int cz, const Ctx2<QQ, 
     return s;
 }
 
-// collide_pair of lattice.cuh on node pairs: outputs of directions q and
-// q + 1 (q odd), f' (FP32) or f'/w_q (SCALED).
-template <int QQ, bool SCALED>
-__device__ __forceinline__ void collide_pair2(int q, const Ctx2<QQ, SCALED> &k, V2 &out_q, V2 &out_qbar) {
+// collide_pair of lattice.cuh on node pairs: post-collision f' of directions
+// q and q + 1 (q odd).
+template <int QQ>
+__device__ __forceinline__ void collide_pair2(int q, const Ctx2<QQ> &k, V2 &out_q, V2 &out_qbar) {
     const int cx = kCX[q], cy = kCY[q], cz = kCZ[q];
-    const int cl = SCALED ? 0 : weight_class(q);
+    const int cl = weight_class(q);
     const double wd = weight<QQ>(q);
-    const V2 nw(SCALED ? -1.0f : -static_cast<float>(wd));
-    const V2 hw(SCALED ? 1.5f : static_cast<float>(1.5 * wd));
+    const V2 nw(-static_cast<float>(wd));
+    const V2 hw(static_cast<float>(1.5 * wd));
     const V2 cu = cdot2(cx, cy, cz, k.u3x, k.u3y, k.u3z);
     const V2 cF = cdot2(cx, cy, cz, k.fx, k.fy, k.fz);
     V2 E = fma2(k.wr[cl], fma2(V2(0.5f) * cu, cu, k.A), nw);
-    E = fma2(k.ow[cl], cpic2<QQ, SCALED>(cx, cy, cz, k), E);
+    E = fma2(k.ow[cl], cpic2<QQ>(cx, cy, cz, k), E);
     E = fma2(hw, fma2(cu, cF, k.nuF), E);
     V2 O;
     if constexpr (QQ == 27) {
         O = fma2(k.wr[cl] * cu, fma2(V2(static_cast<float>(1.0 / 6.0)) * cu, cu, k.A), hw * cF);
-        O = fma2(k.ow[cl], hermite3_2<QQ, SCALED>(cx, cy, cz, k), O);
+        O = fma2(k.ow[cl], hermite3_2<QQ>(cx, cy, cz, k), O);
     } else {
         O = fma2(k.wr[cl], cu, hw * cF);
     }
@@ -308,11 +309,11 @@ __device__ __forceinline__ void collide_pair2(int q, const Ctx2<QQ, SCALED> &k, 
     out_qbar = E - O;
 }
 
-template <int QQ, bool SCALED>
-__device__ __forceinline__ V2 collide_rest2(const Ctx2<QQ, SCALED> &k) {
+template <int QQ>
+__device__ __forceinline__ V2 collide_rest2(const Ctx2<QQ> &k) {
     const double w0 = weight<QQ>(0);
-    const V2 nw(SCALED ? -1.0f : -static_cast<float>(w0));
-    const V2 hw(SCALED ? 1.5f : static_cast<float>(1.5 * w0));
+    const V2 nw(-static_cast<float>(w0));
+    const V2 hw(static_cast<float>(1.5 * w0));
     return fma2(hw, k.nuF, fma2(k.wr[0], k.A, nw));
 }
 
@@ -325,7 +326,7 @@ template <int QQ, bool JET, class S>
 __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const StepBuffers<S, float> &b, int xa,
                                                   int y, int z, bool act_a, bool act_b, const V2 (&pop)[QQ], V2 phi,
                                                   V2 n_x, V2 n_y, V2 n_z, V2 ind, V2 curvature) {
-    constexpr bool SCALED = PairStore<S>::kScaled;
+    constexpr bool FAST = PairStore<S>::kScaled;  // 16-bit storage: approximate reciprocals
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N;
     const uint32_t plane = p.plane;
@@ -335,7 +336,7 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
     const V2 st = V2(-p.sigma) * curvature * ind;
     const V2 fx = st * n_x, fy = st * n_y, fz = st * n_z;
 
-    const Macro2 m = moments2<QQ, SCALED>(pop, fx, fy, fz);
+    const Macro2 m = moments2<QQ, FAST>(pop, fx, fy, fz);
 
     if constexpr (JET) {
         if (z == nz - 2 || z == 1) {
@@ -409,11 +410,11 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
         const float r = sponge_ramp<float>(p, z);
         const V2 visc_local = fma2(phi, V2(p.visc_oil), omp * V2(p.visc_water));
         const V2 tau_zmax = fma2(V2(3.0f), visc_local * V2(p.kgain1), V2(0.5f));
-        omega = recip2<SCALED>(fma2(V2(r), tau_zmax - tau_phi, tau_phi));
+        omega = recip2<FAST>(fma2(V2(r), tau_zmax - tau_phi, tau_phi));
     } else {
         omega = V2(p.omega_ref);
     }
-    const Ctx2<QQ, SCALED> k = make_ctx2<QQ, SCALED>(m, fx, fy, fz, V2(1.0f) - omega);
+    const Ctx2<QQ> k = make_ctx2<QQ>(m, fx, fy, fz, V2(1.0f) - omega);
 
     // collision (src/lbm.cu:172-207) and pull-layout stores, P = wrap(S + c) - c
     // (32-bit node offsets, as in collide_node)
@@ -432,13 +433,14 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
             if (kCY[q] < 0) d += ey_m;
             if (kCZ[q] > 0) d += ez_p;
             if (kCZ[q] < 0) d += ez_m;
-            if (PFLBM_GUARD(d + 1 < N, b.err)) PairStore<S>::store2(b.f_dst + uint64_t(q) * N + d, v);
+            if (PFLBM_GUARD(d + 1 < N, b.err))
+                PairStore<S>::store2(b.f_dst + uint64_t(q) * N + d, v, static_cast<float>(1.0 / weight<QQ>(q)));
         };
-        put(0, collide_rest2<QQ, SCALED>(k));
+        put(0, collide_rest2<QQ>(k));
 #pragma unroll
         for (int q = 1; q < QQ; q += 2) {
             V2 a, c;
-            collide_pair2<QQ, SCALED>(q, k, a, c);
+            collide_pair2<QQ>(q, k, a, c);
             put(q, a);
             put(q + 1, c);
         }
@@ -457,13 +459,14 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
             if (kCZ[q] > 0) d += ez_p;
             if (kCZ[q] < 0) d += ez_m;
             if (PFLBM_GUARD(d < N, b.err))
-                PairStore<S>::store1(b.f_dst + uint64_t(q) * N + d, lb ? v.v.y : v.v.x);
+                PairStore<S>::store1(b.f_dst + uint64_t(q) * N + d, lb ? v.v.y : v.v.x,
+                                     static_cast<float>(1.0 / weight<QQ>(q)));
         };
-        put(0, collide_rest2<QQ, SCALED>(k));
+        put(0, collide_rest2<QQ>(k));
 #pragma unroll
         for (int q = 1; q < QQ; q += 2) {
             V2 a, c;
-            collide_pair2<QQ, SCALED>(q, k, a, c);
+            collide_pair2<QQ>(q, k, a, c);
             put(q, a);
             put(q + 1, c);
         }
