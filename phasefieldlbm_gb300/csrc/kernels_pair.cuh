@@ -65,9 +65,16 @@ struct V2 {
 __device__ __forceinline__ V2 operator+(V2 a, V2 b) { return V2(__fadd2_rn(a.v, b.v)); }
 __device__ __forceinline__ V2 operator*(V2 a, V2 b) { return V2(__fmul2_rn(a.v, b.v)); }
 __device__ __forceinline__ V2 fma2(V2 a, V2 b, V2 c) { return V2(__ffma2_rn(a.v, b.v, c.v)); }
-// a - b as a + (-1) b: one packed instruction, exactly rounded like a subtraction
-__device__ __forceinline__ V2 operator-(V2 a, V2 b) { return fma2(b, V2(-1.0f), a); }
-__device__ __forceinline__ V2 operator-(V2 a) { return a * V2(-1.0f); }
+// packed subtraction (PTX sub.rn.f32x2; the CUDA headers declare only the
+// fma/add/mul forms)
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;"
+        : "=l"(r)
+        : "l"(*reinterpret_cast<const unsigned long long *>(&a.v)), "l"(*reinterpret_cast<const unsigned long long *>(&b.v)));
+    return V2(*reinterpret_cast<const float2 *>(&r));
+}
+__device__ __forceinline__ V2 operator-(V2 a) { return V2(0.0f) - a; }
 __device__ __forceinline__ V2 &operator+=(V2 &a, V2 b) { return a = a + b; }
 // 1/a per lane: IEEE division, or (FAST, 16-bit storage, where the stored
 // value carries 11 or 8 significant bits) the hardware approximate reciprocal
