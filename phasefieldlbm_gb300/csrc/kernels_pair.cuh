@@ -20,8 +20,9 @@
 // jet steps. The exact scaled values round to 16 bits coherently, where the
 // unscaled form's FP32 rounding dithers them.)
 //
-// Used for the plain step (no time averages, no closure) with FP32, FP16 or
-// BF16 storage; the TMA row alignment already makes nx even.
+// The plain step of 16-bit D3Q19 storage runs it (no time averages, no
+// closure); FP32 and D3Q27 can select it (PFLBM_PAIR=1) but are faster with
+// one node per thread. The TMA row alignment already makes nx even.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
