@@ -301,14 +301,8 @@ __device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> 
                 auto v = [&](int dx, int dy, int dz) -> T {
                     return s_phi[dz < 0 ? sm : (dz > 0 ? sp : s0)][ly + 1 + dy][lx + 1 + dx];
                 };
-                const T gxv = T(3) * lattice_grad<QQ, 0, T>(v);
-                const T gyv = T(3) * lattice_grad<QQ, 1, T>(v);
-                const T gzv = T(3) * lattice_grad<QQ, 2, T>(v);
-                ind = sqrt(gxv * gxv + gyv * gyv + gzv * gzv);
-                const T inv = T(1) / (ind + static_cast<T>(1e-9));
-                nxv = gxv * inv;
-                nyv = gyv * inv;
-                nzv = gzv * inv;
+                unit_normal<false>(lattice_grad<QQ, 0, T>(v), lattice_grad<QQ, 1, T>(v), lattice_grad<QQ, 2, T>(v), nxv,
+                                   nyv, nzv, ind);
             }
             s_n[0][sn][ly][lx] = nxv;
             s_n[1][sn][ly][lx] = nyv;

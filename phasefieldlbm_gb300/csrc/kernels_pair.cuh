@@ -28,13 +28,13 @@
 #include <cuda_fp16.h>
 
 #include "kernels_tma.cuh"
+#include "packed.cuh"
 
 namespace pflbm {
 
 constexpr int TX2 = TX / 2;   // threads along x of a tile
 constexpr int NT2 = NT / 2;   // threads of a tile
-constexpr int NXP = NX_ / 2;  // node pairs per row of the normal ring
-static_assert(TX % 2 == 0 && NX_ % 2 == 0, "pair tiles");
+static_assert(TX % 2 == 0, "pair tiles");
 
 // Resident CTAs per SM of the pair kernel and the deepest pipeline that
 // fits them (228 KB of shared memory per SM, 1 KB of it reserved per CTA):
@@ -52,39 +52,6 @@ struct PairStages {
 };
 template <int QQ, class S>
 using PairLayout = TmaPlan<QQ, S, PairStages<QQ, S>::value>;
-
-// Two FP32 lanes, one per node of the pair.
-struct V2 {
-    float2 v;
-    V2() = default;
-    __device__ __forceinline__ V2(float2 a) : v(a) {}
-    __device__ __forceinline__ V2(float a, float b) : v(make_float2(a, b)) {}
-    __device__ __forceinline__ explicit V2(float s) : v(make_float2(s, s)) {}
-    __device__ __forceinline__ explicit V2(double s) : v(make_float2(float(s), float(s))) {}
-    __device__ __forceinline__ explicit V2(int s) : v(make_float2(float(s), float(s))) {}
-};
-__device__ __forceinline__ V2 operator+(V2 a, V2 b) { return V2(__fadd2_rn(a.v, b.v)); }
-__device__ __forceinline__ V2 operator*(V2 a, V2 b) { return V2(__fmul2_rn(a.v, b.v)); }
-__device__ __forceinline__ V2 fma2(V2 a, V2 b, V2 c) { return V2(__ffma2_rn(a.v, b.v, c.v)); }
-// packed subtraction (PTX sub.rn.f32x2; the CUDA headers declare only the
-// fma/add/mul forms)
-__device__ __forceinline__ V2 operator-(V2 a, V2 b) {
-    unsigned long long r;
-    asm("sub.rn.f32x2 %0, %1, %2;"
-        : "=l"(r)
-        : "l"(*reinterpret_cast<const unsigned long long *>(&a.v)), "l"(*reinterpret_cast<const unsigned long long *>(&b.v)));
-    return V2(*reinterpret_cast<const float2 *>(&r));
-}
-__device__ __forceinline__ V2 operator-(V2 a) { return V2(0.0f) - a; }
-__device__ __forceinline__ V2 &operator+=(V2 &a, V2 b) { return a = a + b; }
-// 1/a per lane: IEEE division, or (FAST, 16-bit storage, where the stored
-// value carries 11 or 8 significant bits) the hardware approximate reciprocal
-// of __fdividef, good to about 2 ulp of FP32
-template <bool FAST>
-__device__ __forceinline__ V2 recip2(V2 a) {
-    if constexpr (FAST) return V2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y));
-    else return V2(1.0f / a.v.x, 1.0f / a.v.y);
-}
 
 // ---------------------------------------------------------------- storage
 template <class S>
@@ -551,32 +518,12 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
             const bool yok = zok && gy >= 1 && gy <= ny - 2;
             const bool va = yok && gxa >= 1 && gxa <= nx - 2;
             const bool vb = yok && gxa + 1 >= 1 && gxa + 1 <= nx - 2;
-            V2 nxv(0.0f), nyv(0.0f), nzv(0.0f), indv(0.0f);
-            if (va || vb) {
-                auto v = [&](int dx, int dy, int dz) -> V2 {
-                    const int slot = dz < 0 ? sm : (dz > 0 ? sp : sn);
-                    const T *e = &phi_at(slot, ly + 1 + dy, lx + L::PXO - 1 + dx);
-                    if (dx == 0) return V2(e[0], e[1]);
-                    return V2(*reinterpret_cast<const float2 *>(e));
-                };
-                const V2 gxv = V2(3.0f) * lattice_grad<QQ, 0, V2>(v);
-                const V2 gyv = V2(3.0f) * lattice_grad<QQ, 1, V2>(v);
-                const V2 gzv = V2(3.0f) * lattice_grad<QQ, 2, V2>(v);
-                const V2 g2 = fma2(gxv, gxv, fma2(gyv, gyv, gzv * gzv));
-                indv = V2(sqrtf(g2.v.x), sqrtf(g2.v.y));
-                const V2 inv = recip2<PairStore<S>::kScaled>(indv + V2(1e-9f));
-                nxv = gxv * inv;
-                nyv = gyv * inv;
-                nzv = gzv * inv;
-                if (!(va && vb)) {
-                    if (!va) {
-                        nxv.v.x = 0.0f; nyv.v.x = 0.0f; nzv.v.x = 0.0f; indv.v.x = 0.0f;
-                    }
-                    if (!vb) {
-                        nxv.v.y = 0.0f; nyv.v.y = 0.0f; nzv.v.y = 0.0f; indv.v.y = 0.0f;
-                    }
-                }
-            }
+            V2 nxv, nyv, nzv, indv;
+            normal_pair<QQ, PairStore<S>::kScaled>(
+                [&](int dx, int dy, int dz) -> const T * {
+                    return &phi_at(dz < 0 ? sm : (dz > 0 ? sp : sn), ly + 1 + dy, lx + L::PXO - 1 + dx);
+                },
+                va, vb, nxv, nyv, nzv, indv);
             *reinterpret_cast<float2 *>(&n_at(0, nn, ly, lx)) = nxv.v;
             *reinterpret_cast<float2 *>(&n_at(1, nn, ly, lx)) = nyv.v;
             *reinterpret_cast<float2 *>(&n_at(2, nn, ly, lx)) = nzv.v;

@@ -22,11 +22,41 @@
 // whole, so a failure never hangs the GPU.
 #pragma once
 #include "kernels.cuh"
+#include "packed.cuh"
 #include "tma.cuh"
 
 namespace pflbm {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr int NXP = NX_ / 2;  // x-adjacent entry pairs per row of the normal ring
+static_assert(NX_ % 2 == 0, "normal ring pairs");
+
+// n^ and |grad phi| of the normal-ring entries (lx, ly) and (lx + 1, ly), lx
+// even, with packed FP32x2 arithmetic: `e(dx, dy, dz)` points at the phi
+// element of the first entry's neighbour (dx, dy, dz). The +-1 x neighbours
+// of an even pair are aligned 8-byte words; the dx = 0 column takes two
+// loads. A lane whose node is not interior (va / vb false) gets zeros. Same
+// rounding as the scalar unit_normal (stencil.cuh).
+template <int QQ, bool FAST, class Elem>
+__device__ __forceinline__ void normal_pair(const Elem &e, bool va, bool vb, V2 &nxv, V2 &nyv, V2 &nzv, V2 &indv) {
+    nxv = nyv = nzv = indv = V2(0.0f);
+    if (!(va || vb)) return;
+    auto v = [&](int dx, int dy, int dz) -> V2 {
+        const float *q = e(dx, dy, dz);
+        if (dx == 0) return V2(q[0], q[1]);
+        return V2(*reinterpret_cast<const float2 *>(q));
+    };
+    unit_normal<FAST>(lattice_grad<QQ, 0, V2>(v), lattice_grad<QQ, 1, V2>(v), lattice_grad<QQ, 2, V2>(v), nxv, nyv,
+                      nzv, indv);
+    if (!(va && vb)) {
+        if (!va) {
+            nxv.v.x = 0.0f; nyv.v.x = 0.0f; nzv.v.x = 0.0f; indv.v.x = 0.0f;
+        }
+        if (!vb) {
+            nxv.v.y = 0.0f; nyv.v.y = 0.0f; nzv.v.y = 0.0f; indv.v.y = 0.0f;
+        }
+    }
+}
 
 __host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~size_t(127); }
 
@@ -175,27 +205,42 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
     auto compute_n = [&](int zp) {
         const int sn = pslot(zp), sm = pslot(zp - 1), sp = pslot(zp + 1);
         const int nn = (zp + 4) & 3;  // normal ring slot
-        for (int i = tid; i < NX_ * NY_; i += NT) {
-            const int lx = i % NX_, ly = i / NX_;
-            const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
-            T nxv = T(0), nyv = T(0), nzv = T(0), ind = T(0);
-            if (gx >= 1 && gx <= nx - 2 && gy >= 1 && gy <= ny - 2 && zp >= 1 && zp <= nz - 2) {
-                auto v = [&](int dx, int dy, int dz) -> T {
-                    return phi_at(dz < 0 ? sm : (dz > 0 ? sp : sn), ly + 1 + dy, lx + L::PXO - 1 + dx);
-                };
-                const T gxv = T(3) * lattice_grad<QQ, 0, T>(v);
-                const T gyv = T(3) * lattice_grad<QQ, 1, T>(v);
-                const T gzv = T(3) * lattice_grad<QQ, 2, T>(v);
-                ind = sqrt(gxv * gxv + gyv * gyv + gzv * gzv);
-                const T inv = T(1) / (ind + static_cast<T>(1e-9));
-                nxv = gxv * inv;
-                nyv = gyv * inv;
-                nzv = gzv * inv;
+        if constexpr (sizeof(T) == 4) {
+            // two x-adjacent entries per thread: 170 entry pairs, at most one
+            // per thread, so no warp computes a second round
+            const bool zok = zp >= 1 && zp <= nz - 2;
+            for (int i = tid; i < NXP * NY_; i += NT) {
+                const int lx = 2 * (i % NXP), ly = i / NXP;
+                const int gxa = x0 - 1 + lx, gy = y0 - 1 + ly;
+                const bool yok = zok && gy >= 1 && gy <= ny - 2;
+                V2 nxv, nyv, nzv, ind;
+                normal_pair<QQ, false>(
+                    [&](int dx, int dy, int dz) -> const float * {
+                        return &phi_at(dz < 0 ? sm : (dz > 0 ? sp : sn), ly + 1 + dy, lx + L::PXO - 1 + dx);
+                    },
+                    yok && gxa >= 1 && gxa <= nx - 2, yok && gxa + 1 >= 1 && gxa + 1 <= nx - 2, nxv, nyv, nzv, ind);
+                *reinterpret_cast<float2 *>(&n_at(0, nn, ly, lx)) = nxv.v;
+                *reinterpret_cast<float2 *>(&n_at(1, nn, ly, lx)) = nyv.v;
+                *reinterpret_cast<float2 *>(&n_at(2, nn, ly, lx)) = nzv.v;
+                if (ly >= 1 && ly <= TY) *reinterpret_cast<float2 *>(&ind_at(zp, ly - 1, lx)) = ind.v;
             }
-            n_at(0, nn, ly, lx) = nxv;
-            n_at(1, nn, ly, lx) = nyv;
-            n_at(2, nn, ly, lx) = nzv;
-            if (ly >= 1 && ly <= TY) ind_at(zp, ly - 1, lx) = ind;
+        } else {
+            for (int i = tid; i < NX_ * NY_; i += NT) {
+                const int lx = i % NX_, ly = i / NX_;
+                const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+                T nxv = T(0), nyv = T(0), nzv = T(0), ind = T(0);
+                if (gx >= 1 && gx <= nx - 2 && gy >= 1 && gy <= ny - 2 && zp >= 1 && zp <= nz - 2) {
+                    auto v = [&](int dx, int dy, int dz) -> T {
+                        return phi_at(dz < 0 ? sm : (dz > 0 ? sp : sn), ly + 1 + dy, lx + L::PXO - 1 + dx);
+                    };
+                    unit_normal<false>(lattice_grad<QQ, 0, T>(v), lattice_grad<QQ, 1, T>(v), lattice_grad<QQ, 2, T>(v),
+                                       nxv, nyv, nzv, ind);
+                }
+                n_at(0, nn, ly, lx) = nxv;
+                n_at(1, nn, ly, lx) = nyv;
+                n_at(2, nn, ly, lx) = nzv;
+                if (ly >= 1 && ly <= TY) ind_at(zp, ly - 1, lx) = ind;
+            }
         }
     };
     __syncthreads();

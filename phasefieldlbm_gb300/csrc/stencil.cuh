@@ -9,6 +9,28 @@
 
 namespace pflbm {
 
+// Correctly rounded elementary operations (never contracted), so that the
+// scalar stencils and their packed two-lane form (V2, packed.cuh) round
+// identically and the kernels built on either agree bit for bit. The
+// compiler fuses a packed multiply followed by a packed add into one FFMA2
+// even when both carry .rn, so the stencils below never feed a product into
+// an addition: every multiply-add is written as op_fma.
+__device__ __forceinline__ float op_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double op_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float op_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double op_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float op_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double op_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float op_sqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double op_sqrt(double a) { return sqrt(a); }
+template <bool FAST>
+__device__ __forceinline__ float op_recip(float a) {
+    if constexpr (FAST) return __fdividef(1.0f, a);
+    else return 1.0f / a;
+}
+template <bool FAST>
+__device__ __forceinline__ double op_recip(double a) { return 1.0 / a; }
+
 namespace detail {
 // Direction components as constant expressions (same table as kCX/kCY/kCZ),
 // so that every stencil offset below is resolved at compile time.
@@ -53,9 +75,23 @@ __device__ __forceinline__ T lattice_grad(const Get &v) {
     T s[3] = {T(0), T(0), T(0)};
     bool first[3] = {true, true, true};
     detail::grad_pairs<AXIS>(v, s, first, std::make_integer_sequence<int, (QQ - 1) / 2>{});
-    T r = static_cast<T>(Weights<QQ>::w1) * s[0] + static_cast<T>(Weights<QQ>::w2) * s[1];
-    if constexpr (QQ == 27) r += static_cast<T>(Weights<QQ>::w3) * s[2];
+    T r = op_fma(static_cast<T>(Weights<QQ>::w1), s[0], op_mul(static_cast<T>(Weights<QQ>::w2), s[1]));
+    if constexpr (QQ == 27) r = op_fma(static_cast<T>(Weights<QQ>::w3), s[2], r);
     return r;
+}
+
+// Interface normal n = grad phi / (|grad phi| + 1e-9) and |grad phi| from
+// the lattice gradient sums (src/phaseField.cuh:67-118), in one fixed
+// rounding order for the scalar and packed evaluations.
+template <bool FAST, class T>
+__device__ __forceinline__ void unit_normal(T sx, T sy, T sz, T &nx, T &ny, T &nz, T &ind) {
+    const T gx = op_mul(static_cast<T>(3.0), sx), gy = op_mul(static_cast<T>(3.0), sy),
+            gz = op_mul(static_cast<T>(3.0), sz);
+    ind = op_sqrt(op_fma(gx, gx, op_fma(gy, gy, op_mul(gz, gz))));
+    const T inv = op_recip<FAST>(op_add(ind, static_cast<T>(1e-9)));
+    nx = op_mul(gx, inv);
+    ny = op_mul(gy, inv);
+    nz = op_mul(gz, inv);
 }
 
 }  // namespace pflbm
