@@ -188,6 +188,17 @@ class EngineT final : public Engine {
             return;
         }
         use_tma_ = true;
+        // the closure modes on the TMA kernel (network after the pipeline's
+        // shared memory); without room they stay on the plain-load kernel
+        tma_closure_ = false;
+        if constexpr (sizeof(S) >= 4) {
+            const int smc = int(L::total + closure_smem_bytes<T>());
+            tma_closure_ = cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, smc) == cudaSuccess &&
+                           cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE_AVG>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, smc) == cudaSuccess;
+            if (!tma_closure_) cudaGetLastError();
+        }
         // two nodes per thread with packed FP32x2 arithmetic for the plain
         // step of 16-bit D3Q19 storage, whose collide is issue-bound (FP32
         // and D3Q27 stay faster with one node per thread and twice the
@@ -253,9 +264,16 @@ class EngineT final : public Engine {
         const StepBuffers<S, T> b = buffers(parity);
         if (ev) cudaEventRecord(ev[0], s);
         if (closure_) {
-            // learned closure: plain-load kernel with the network in shared memory
+            // learned closure: the network in shared memory
             if constexpr (sizeof(S) >= 4) {
-                if (avg_)
+                const size_t smc = TmaLayout<QQ, S>::total + closure_smem_bytes<T>();
+                if (use_tma_ && tma_closure_ && avg_)
+                    k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE_AVG>
+                        <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+                else if (use_tma_ && tma_closure_)
+                    k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE>
+                        <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+                else if (avg_)
                     k_collide<QQ, JET, S, MODE_STEP_CLOSURE_AVG><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
                 else
                     k_collide<QQ, JET, S, MODE_STEP_CLOSURE><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
@@ -391,6 +409,7 @@ class EngineT final : public Engine {
     unsigned int *err_ = nullptr;
     bool use_tma_ = false;
     bool use_pair_ = false;  // k_collide_pair for the plain step
+    bool tma_closure_ = false;  // closure modes on k_collide_tma
     bool no_vec_ = false;  // PFLBM_NO_VEC=1: scalar phase kernel
     float *mlp_ = nullptr;  // closure network blob (kMlpBlob floats)
     bool closure_ = false;

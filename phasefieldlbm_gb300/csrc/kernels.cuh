@@ -78,6 +78,17 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
     // node index, 32-bit (N < 2^32 is checked on the host)
     const uint32_t node = uint32_t(x) + uint32_t(nx) * (uint32_t(y) + uint32_t(ny) * uint32_t(z));
     const uint64_t base = node;
+    // running averages of this node, loaded before any store of the node
+    // (the compiler cannot move them above the population stores, which it
+    // cannot prove do not alias them), so their latency overlaps the
+    // collision instead of following it
+    T av_old[10];
+    if constexpr (mode_average(MODE)) {
+        if (active && PFLBM_GUARD(base < N, b.err)) {
+#pragma unroll
+            for (int k = 0; k < 10; ++k) av_old[k] = b.avg[k * N + base];
+        }
+    }
     const T st = -p.sigma * curvature * ind;
     const T fx = st * n_x, fy = st * n_y, fz = st * n_z;
 
@@ -222,16 +233,10 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
                 const T o = av[slot * N + i];
                 av[slot * N + i] = o + (nv_ - o) / tf;
             };
-            upd(0, base, phi);
-            upd(1, base, m.ux);
-            upd(2, base, m.uy);
-            upd(3, base, m.uz);
-            upd(4, base, m.ux * m.ux);
-            upd(5, base, m.uy * m.uy);
-            upd(6, base, m.uz * m.uz);
-            upd(7, base, m.ux * m.uy);
-            upd(8, base, m.ux * m.uz);
-            upd(9, base, m.uy * m.uz);
+            const T now[10] = {phi, m.ux, m.uy, m.uz, m.ux * m.ux, m.uy * m.uy, m.uz * m.uz,
+                               m.ux * m.uy, m.ux * m.uz, m.uy * m.uz};
+#pragma unroll
+            for (int k = 0; k < 10; ++k) av[k * N + base] = av_old[k] + (now[k] - av_old[k]) / tf;
             if constexpr (JET) {
                 if (z == 1 && in_disc<T>(p, x, y)) {
                     // ghost inlet node (x,y,0) holds phi = 1 and the inlet velocity

@@ -102,6 +102,13 @@ struct TmaPlan {
 #define PFLBM_TMA_SMEM_BUDGET (113u * 1024u)  // per CTA: two CTAs per SM
 #endif
 
+// Shared bytes the closure modes add after the TMA plan: the network blob,
+// and for FP32 its mma fragments and per-warp feature tiles.
+template <class T>
+constexpr size_t closure_smem_bytes() {
+    return sizeof(float) * size_t(sizeof(T) == 4 ? mlp_smem_words(NT / 32) : kMlpBlob);
+}
+
 // Resident CTAs per SM of the TMA collide: one for FP64; three for D3Q19
 // with 16-bit storage, which is issue-bound rather than bandwidth-bound and
 // gains more from the extra warps (80 registers) than it loses to the
@@ -146,7 +153,8 @@ template <int QQ, bool JET, class S, int MODE>
 __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>::T> &p,
                                                  const StepBuffers<S, typename Store<S>::T> &b,
                                                  const CUtensorMap *fmap_p, const CUtensorMap *phimap_p, int x0,
-                                                 int y0, int zb, int ze, unsigned char *smem, uint32_t &seq) {
+                                                 int y0, int zb, int ze, unsigned char *smem, uint32_t &seq,
+                                                 float *s_mlp = nullptr) {
     using T = typename Store<S>::T;
     using L = TmaLayout<QQ, S>;
     S *s_f = reinterpret_cast<S *>(smem + L::off_f);
@@ -270,7 +278,9 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         }
         // plane z+NS-1 goes into the stage of plane z-1, consumed last iteration
         if (tid == 0 && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
-        if (!col) continue;
+        // the tensor-core closure network needs every lane of the warp
+        constexpr bool kWarpWide = mode_closure(MODE) && std::is_same<T, float>::value;
+        if (!col && !kWarpWide) continue;
 
         const int s_m = (z + 3) & 3, s_0 = z & 3, s_p = (z + 1) & 3;
         auto nv = [&](int c, int dx, int dy, int dz) -> T {
@@ -286,11 +296,17 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         T pop[QQ];
         const unsigned char *sf = reinterpret_cast<const unsigned char *>(s_f) + size_t(st) * L::stage_bytes +
                                   (size_t(ty) * L::BW + tx + L::XO) * sizeof(S);
+        if (kWarpWide && !col) {
 #pragma unroll
-        for (int q = 0; q < QQ; ++q)
-            pop[q] = Store<S>::widen(*reinterpret_cast<const S *>(sf + size_t(q) * L::box_stride - kCX[q] * int(sizeof(S))),
-                                     static_cast<T>(weight<QQ>(q)));
-        collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature);
+            for (int q = 0; q < QQ; ++q) pop[q] = T(0);  // placeholder node of the warp-wide network
+        } else {
+#pragma unroll
+            for (int q = 0; q < QQ; ++q)
+                pop[q] = Store<S>::widen(
+                    *reinterpret_cast<const S *>(sf + size_t(q) * L::box_stride - kCX[q] * int(sizeof(S))),
+                    static_cast<T>(weight<QQ>(q)));
+        }
+        collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature, s_mlp, col);
     }
     seq += uint32_t(ze - zb);
     return true;
@@ -301,12 +317,24 @@ __global__ void __launch_bounds__(NT, CollideOccupancy<QQ, S>::value)
     k_collide_tma(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b,
                   const __grid_constant__ CUtensorMap fmap, const __grid_constant__ CUtensorMap phimap) {
     extern __shared__ __align__(128) unsigned char smem[];
+    float *s_mlp = nullptr;
+    if constexpr (mode_closure(MODE)) {
+        // closure network after the pipeline's shared memory (kernels.cuh's k_collide does the same)
+        static_assert(TX == 32, "the tensor-core network maps one warp to one tile row");
+        s_mlp = reinterpret_cast<float *>(smem + TmaLayout<QQ, S>::total);
+        for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpBlob; i += NT) s_mlp[i] = b.mlp[i];
+        __syncthreads();
+        if constexpr (std::is_same<typename Store<S>::T, float>::value) {
+            mlp_build_fragments(s_mlp, threadIdx.x + TX * threadIdx.y, NT);
+            __syncthreads();
+        }
+    }
     tma_pipeline_init<QQ, S>(smem);
     const int zb = 1 + blockIdx.z * p.zchunk;
     const int ze = min(zb + p.zchunk, int(p.nz) - 1);
     uint32_t seq = 0;
     collide_tile_tma<QQ, JET, S, MODE>(p, b, &fmap, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb, ze, smem,
-                                       seq);
+                                       seq, s_mlp);
 }
 
 }  // namespace pflbm

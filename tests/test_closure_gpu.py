@@ -277,3 +277,35 @@ def test_trained_closure_beats_constant_tau(pflbm):
     print("training loss", l0, "->", l1, "errors", err)
     assert err["closure"]["avg_uz"] < err["plain"]["avg_uz"]
     assert err["closure"]["avg_phi"] < 1.01 * err["plain"]["avg_phi"]
+
+
+@pytest.mark.parametrize("storage,avg", [(0, 0), (0, 1), (3, 0)])
+def test_closure_on_tma_and_plain_kernels_bit_identical(pflbm, monkeypatch, storage, avg):
+    """The closure-coupled step runs on the TMA-fed collide when rows are
+    16-byte aligned (network after the pipeline's shared memory) and on the
+    plain-load kernel otherwise; both give the same bits (FP32: tensor-core
+    network, all 32 lanes of a warp taking part; FP64: per-thread network;
+    avg: the closure step that also updates the time averages)."""
+    cfg = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
+    cfg.nx, cfg.ny, cfg.nz, cfg.diam, cfg.radius = 64, 40, 48, 10, 5
+    cfg.inflow_noise, cfg.noise_amp, cfg.seed = pflbm.NOISE_UNIFORM_UZ, 0.05, 12345
+    cfg.storage = storage
+    if avg:
+        cfg.flags = pflbm.FLAG_TIME_AVERAGE | pflbm.FLAG_REYNOLDS_MOMENTS
+    with pflbm.Closure(4096) as c:
+        c.set_samples(_features(4096, 7), np.full(4096, 2e-3))
+        c.init_params(seed=9)
+        blob = c.blob.copy()
+    blob[:1377] += np.random.default_rng(8).normal(0.0, 0.1, 1377).astype(np.float32)
+    fields = ("rho", "ux", "uy", "uz", "phi", "pxx", "fsx") + (("avg_uz", "avg_uzuz") if avg else ())
+    out = {}
+    for mode in ("tma", "plain"):
+        if mode == "plain":
+            monkeypatch.setenv("PFLBM_NO_TMA", "1")
+        with pflbm.Simulation(cfg) as s:
+            assert s.uses_tma == (mode == "tma")
+            s.set_closure(blob, strength=1.0)
+            s.step(25)
+            out[mode] = {f: s.get_field(f, dtype=np.float64) for f in fields}
+    for f in fields:
+        assert np.array_equal(out["tma"][f], out["plain"][f]), f
