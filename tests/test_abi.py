@@ -115,3 +115,14 @@ int main(void) {
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert "nz >= 12" in r.stdout
+
+
+def test_create_rejects_grids_of_2_32_nodes(pflbm):
+    # the step kernels index a node within one array with 32 bits
+    lib = pflbm.load_library()
+    c = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
+    c.nx, c.ny, c.nz = 2048, 2048, 1024
+    h = ctypes.c_void_p()
+    assert lib.pflbm_create(ctypes.byref(c), ctypes.byref(h)) == 1
+    assert "2^32" in lib.pflbm_last_error().decode()
+    assert not h.value
