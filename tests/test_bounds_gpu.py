@@ -71,3 +71,36 @@ def test_checked_build_fires_no_guard_and_matches(pflbm):
                 assert int(ens.reduce(k).nonfinite) == 0
     finally:
         pflbm._LIB = normal
+
+
+def test_checked_build_closure_step(pflbm):
+    """The closure-coupled step (TMA collide with the network after the
+    pipeline's shared memory, time averages on) under the bounds-checked
+    build: no guard fires and the fields equal the normal build's to
+    rounding."""
+    from phasefieldlbm_gb300 import build
+
+    rng = np.random.default_rng(5)
+    feats = np.empty((2048, 8))
+    feats[:, :6] = rng.normal(0.0, 1e-4, (2048, 6))
+    feats[:, 6] = rng.uniform(0.0, 1.0, 2048)
+    feats[:, 7] = rng.exponential(0.05, 2048)
+    checked = pflbm.load_library(str(build.build_checked()))
+    normal = pflbm.load_library()
+    try:
+        with pflbm.Closure(2048) as c:
+            c.set_samples(feats, np.full(2048, 2e-3))
+            c.init_params(seed=3)
+            blob = c.blob.copy()
+        cfg = pflbm.preset("jet_d3q19", nx=40, ny=36, nz=48, diam=10, radius=5, flags=pflbm.FLAG_TIME_AVERAGE)
+        out = {}
+        for name, lib in (("checked", checked), ("normal", normal)):
+            pflbm._LIB = lib
+            with pflbm.Simulation(cfg) as s:
+                s.set_closure(blob, strength=1.0)
+                s.step(17)  # raises PflbmError if a guard fired
+                out[name] = {f: s.get_field(f, dtype=np.float64) for f in FIELDS + ("avg_uz",)}
+        for f in out["normal"]:
+            assert rel_l2(out["checked"][f], out["normal"][f]) <= 1e-5, f
+    finally:
+        pflbm._LIB = normal
