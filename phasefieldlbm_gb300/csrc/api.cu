@@ -431,6 +431,21 @@ void free_pinned(pflbm_sim *s) {
     s->pinned.clear();
 }
 
+// Frees everything a simulation holds, also one that pflbm_create left
+// half built after an error.
+void release_resources(pflbm_sim *s) {
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->writer.joinable()) s->writer.join();
+    free_pinned(s);
+    destroy_graphs(s);
+    if (s->dev_diag) cudaFree(s->dev_diag);
+    s->dev_diag = nullptr;
+    s->eng.reset();
+    if (s->stream) cudaStreamDestroy(s->stream);
+    s->stream = nullptr;
+}
+
 }  // namespace
 
 extern "C" {
@@ -515,21 +530,23 @@ int pflbm_create(const pflbm_config *cfg, pflbm_sim **out) {
     }
     if (!eng) return fail(PFLBM_ERR_OUT_OF_MEMORY, "engine allocation failed");
     s->eng.reset(eng);
+    // from here on an error releases what was built so far
+    auto abandon = [&](int code) {
+        release_resources(s.get());
+        return code;
+    };
     std::string err;
     rc = s->eng->allocate(err);
-    if (rc) return fail(rc, err);
+    if (rc) return abandon(fail(rc, err));
     e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    if (e != cudaSuccess) return abandon(cuda_fail(e, "cudaStreamCreate"));
     e = cudaMalloc(&s->dev_diag, sizeof(double) * 16);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc diag");
+    if (e != cudaSuccess) return abandon(cuda_fail(e, "cudaMalloc diag"));
     const int counts[3] = {1, 2, kChunk};
     for (int par = 0; par < 2; ++par)
         for (int k = 0; k < 3; ++k) {
             rc = capture(s.get(), par, counts[k], &s->graphs[par][k]);
-            if (rc) {
-                destroy_graphs(s.get());
-                return rc;
-            }
+            if (rc) return abandon(rc);
         }
     *out = s.release();
     return PFLBM_OK;
@@ -947,14 +964,7 @@ int pflbm_kernels_per_step(const pflbm_sim *s, int32_t *count) {
 
 int pflbm_destroy(pflbm_sim *s) {
     if (!s) return PFLBM_OK;
-    cudaSetDevice(s->device);
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    if (s->writer.joinable()) s->writer.join();
-    free_pinned(s);
-    destroy_graphs(s);
-    if (s->dev_diag) cudaFree(s->dev_diag);
-    s->eng.reset();
-    if (s->stream) cudaStreamDestroy(s->stream);
+    release_resources(s);
     delete s;
     return PFLBM_OK;
 }
