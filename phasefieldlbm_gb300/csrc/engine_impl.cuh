@@ -51,11 +51,12 @@ Params<T> make_params(const HostParams &h) {
 }
 
 // Tensor maps of the TMA collide kernel for one grid: f as (x, y, z, q) with
-// boxes (BW, TY, 1, 1), phi as (x, y, z) with boxes (PBW, PBH, 1). False when
-// the driver entry point is missing or the encoder rejects the layout.
+// boxes (BWN, TY, 1, 1) for the c_x = 0 directions and (BWW, TY, 1, 1) for
+// the others, phi as (x, y, z) with boxes (PBW, PBH, 1). False when the
+// driver entry point is missing or the encoder rejects the layout.
 template <int QQ, class S>
 bool encode_collide_maps(const S *f, const typename Store<S>::T *phi, uint64_t nx, uint64_t ny, uint64_t nz,
-                         CUtensorMap &fmap, CUtensorMap &phimap) {
+                         CUtensorMap &fmapn, CUtensorMap &fmapw, CUtensorMap &phimap) {
     using T = typename Store<S>::T;
     using L = TmaLayout<QQ, S>;
     using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -77,12 +78,14 @@ bool encode_collide_maps(const S *f, const typename Store<S>::T *phi, uint64_t n
     const uint64_t N = nx * ny * nz;
     const cuuint64_t fdim[4] = {nx, ny, nz, cuuint64_t(QQ)};
     const cuuint64_t fstr[3] = {nx * sizeof(S), nx * ny * sizeof(S), N * sizeof(S)};
-    const cuuint32_t fbox[4] = {cuuint32_t(L::BW), cuuint32_t(TY), 1, 1};
+    const cuuint32_t fboxn[4] = {cuuint32_t(L::BWN), cuuint32_t(TY), 1, 1};
+    const cuuint32_t fboxw[4] = {cuuint32_t(L::BWW), cuuint32_t(TY), 1, 1};
     const cuuint32_t one4[4] = {1, 1, 1, 1};
-    if (enc(&fmap, ft, 4, const_cast<S *>(f), fdim, fstr, fbox, one4, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return false;
+    for (int k = 0; k < 2; ++k)
+        if (enc(k ? &fmapw : &fmapn, ft, 4, const_cast<S *>(f), fdim, fstr, k ? fboxw : fboxn, one4,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
     const cuuint64_t pdim[3] = {nx, ny, nz};
     const cuuint64_t pstr[2] = {nx * sizeof(T), nx * ny * sizeof(T)};
     const cuuint32_t pbox[3] = {cuuint32_t(L::PBW), cuuint32_t(L::PBH), 1};
@@ -179,7 +182,8 @@ class EngineT final : public Engine {
         if ((uint64_t(h_.nx) * sizeof(S)) % 16 != 0 || (uint64_t(h_.nx) * sizeof(T)) % 16 != 0) return;
         using L = TmaLayout<QQ, S>;
         for (int k = 0; k < 2; ++k)
-            if (!encode_collide_maps<QQ, S>(f_[k], phi_[k], h_.nx, h_.ny, h_.nz, fmap_[k], phimap_[k])) return;
+            if (!encode_collide_maps<QQ, S>(f_[k], phi_[k], h_.nx, h_.ny, h_.nz, fmapn_[k], fmapw_[k], phimap_[k]))
+                return;
         if (cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(L::total)) != cudaSuccess ||
             cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_AVG>,
@@ -269,10 +273,10 @@ class EngineT final : public Engine {
                 const size_t smc = TmaLayout<QQ, S>::total + closure_smem_bytes<T>();
                 if (use_tma_ && tma_closure_ && avg_)
                     k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE_AVG>
-                        <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+                        <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmapn_[parity], fmapw_[parity], phimap_[parity]);
                 else if (use_tma_ && tma_closure_)
                     k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE>
-                        <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+                        <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmapn_[parity], fmapw_[parity], phimap_[parity]);
                 else if (avg_)
                     k_collide<QQ, JET, S, MODE_STEP_CLOSURE_AVG><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
                 else
@@ -282,14 +286,14 @@ class EngineT final : public Engine {
             const size_t sm = TmaLayout<QQ, S>::total;
             if (avg_) {
                 k_collide_tma<QQ, JET, S, MODE_STEP_AVG>
-                    <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+                    <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmapn_[parity], fmapw_[parity], phimap_[parity]);
             } else if (use_pair_) {
                 if constexpr (sizeof(T) == 4)
                     k_collide_pair<QQ, JET, S><<<collide_grid(), dim3(TX2, TY, 1), PairLayout<QQ, S>::total, s>>>(
-                        p_, b, fmap_[parity], phimap_[parity]);
+                        p_, b, fmapn_[parity], fmapw_[parity], phimap_[parity]);
             } else {
                 k_collide_tma<QQ, JET, S, MODE_STEP>
-                    <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmap_[parity], phimap_[parity]);
+                    <<<collide_grid(), dim3(TX, TY, 1), sm, s>>>(p_, b, fmapn_[parity], fmapw_[parity], phimap_[parity]);
             }
         } else if (avg_) {
             k_collide<QQ, JET, S, MODE_STEP_AVG><<<collide_grid(), dim3(TX, TY, 1), 0, s>>>(p_, b);
@@ -413,7 +417,7 @@ class EngineT final : public Engine {
     bool no_vec_ = false;  // PFLBM_NO_VEC=1: scalar phase kernel
     float *mlp_ = nullptr;  // closure network blob (kMlpBlob floats)
     bool closure_ = false;
-    CUtensorMap fmap_[2]{}, phimap_[2]{};
+    CUtensorMap fmapn_[2]{}, fmapw_[2]{}, phimap_[2]{};
     uint64_t bytes_ = 0;
 };
 

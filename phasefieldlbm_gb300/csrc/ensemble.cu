@@ -84,9 +84,11 @@ __global__ void __launch_bounds__(NT, 2)
 // pipeline barriers carry on from tile to tile through `seq`.
 constexpr int kMaxTmaBoxes = 64;
 struct BatchMaps {
-    CUtensorMap f[kMaxTmaBoxes];
+    CUtensorMap fn[kMaxTmaBoxes];  // populations, c_x = 0 boxes
+    CUtensorMap fw[kMaxTmaBoxes];  // populations, c_x != 0 boxes
     CUtensorMap phi[kMaxTmaBoxes];
 };
+static_assert(sizeof(BatchMaps) <= 32764, "kernel parameter limit");
 
 template <int QQ>
 __global__ void __launch_bounds__(NT, 2)
@@ -109,8 +111,8 @@ __global__ void __launch_bounds__(NT, 2)
         const WorkItem w = items[it];
         const BoxDev &bx = boxes[w.box];
         const StepBuffers<float, float> b = box_buffers(bp, bx, parity);
-        if (!collide_tile_tma<QQ, false, float, MODE_STEP>(bx.p, b, &maps.f[w.box], &maps.phi[w.box], w.x0, w.y0,
-                                                          w.zb, w.ze, smem, seq))
+        if (!collide_tile_tma<QQ, false, float, MODE_STEP>(bx.p, b, &maps.fn[w.box], &maps.fw[w.box],
+                                                          &maps.phi[w.box], w.x0, w.y0, w.zb, w.ze, smem, seq))
             return;
         __syncthreads();  // shared rings are reused by the next item
     }
@@ -262,9 +264,11 @@ class Ensemble {
                 const BoxDev &bx = boxes[k];
                 const bool ok =
                     q == 19 ? encode_collide_maps<19, float>(bp.f[par] + bx.f_off, bp.phi[par] + bx.n_off, bx.p.nx,
-                                                            bx.p.ny, bx.p.nz, maps[par]->f[k], maps[par]->phi[k])
+                                                            bx.p.ny, bx.p.nz, maps[par]->fn[k], maps[par]->fw[k],
+                                                            maps[par]->phi[k])
                             : encode_collide_maps<27, float>(bp.f[par] + bx.f_off, bp.phi[par] + bx.n_off, bx.p.nx,
-                                                            bx.p.ny, bx.p.nz, maps[par]->f[k], maps[par]->phi[k]);
+                                                            bx.p.ny, bx.p.nz, maps[par]->fn[k], maps[par]->fw[k],
+                                                            maps[par]->phi[k]);
                 if (!ok) return;
             }
         }

@@ -452,8 +452,9 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
 // same pipeline (stage sequence `seq`, bounded waits, abort path).
 template <int QQ, bool JET, class S>
 __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const StepBuffers<S, float> &b,
-                                                  const CUtensorMap *fmap_p, const CUtensorMap *phimap_p, int x0,
-                                                  int y0, int zb, int ze, unsigned char *smem, uint32_t &seq) {
+                                                  const CUtensorMap *fmapn_p, const CUtensorMap *fmapw_p,
+                                                  const CUtensorMap *phimap_p, int x0, int y0, int zb, int ze,
+                                                  unsigned char *smem, uint32_t &seq) {
     using T = float;
     using L = PairLayout<QQ, S>;
     S *s_f = reinterpret_cast<S *>(smem + L::off_f);
@@ -461,7 +462,9 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);
     T *s_ind = reinterpret_cast<T *>(smem + L::off_ind);
     constexpr int NS = L::kStages, R = L::kPhiSlots;
-    static_assert(L::PXO % 2 == 0 && L::XO % 2 == 0 && L::BW % 2 == 0 && L::PBW % 2 == 0, "pair alignment");
+    // c_x = 0 boxes: element 2 i2 of an even-width row, an aligned pair
+    static_assert(L::PXO % 2 == 0 && L::BWN % 2 == 0 && L::BWW % 2 == 0 && L::XU % 2 == 0 && L::PBW % 2 == 0,
+                  "pair alignment");
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
     volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L::off_bar + 8 * NS);
 
@@ -485,12 +488,14 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
         unsigned char *dst = reinterpret_cast<unsigned char *>(s_f) + size_t(stage) * L::stage_bytes;
 #pragma unroll
         for (int q = 0; q < QQ; ++q)
-            tma_load_4d(dst + size_t(q) * L::box_stride, fmap_p, &bar[stage], x0 - L::XO, y0 - kCY[q], zf - kCZ[q], q);
+            tma_load_4d(dst + L::box_off(q), kCX[q] == 0 ? fmapn_p : fmapw_p, &bar[stage], x0 - L::shift(q),
+                        y0 - kCY[q], zf - kCZ[q], q);
         tma_load_3d(&phi_at(pslot(zf + 2), 0, 0), phimap_p, &bar[stage], x0 - L::PXO, y0 - 2, zf + 2);
     };
 
     if (tid == 0) {
-        tma_prefetch_desc(fmap_p);
+        tma_prefetch_desc(fmapn_p);
+        tma_prefetch_desc(fmapw_p);
         tma_prefetch_desc(phimap_p);
     }
     for (int zp = zb - 2; zp <= zb + 1; ++zp) {
@@ -570,14 +575,12 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
         const V2 phi(*reinterpret_cast<const float2 *>(&phi_at(pslot(z), ty + 2, 2 * i2 + L::PXO)));
 
         V2 pop[QQ];
-        const S *sf = reinterpret_cast<const S *>(reinterpret_cast<const unsigned char *>(s_f) +
-                                                  size_t(st) * L::stage_bytes) +
-                      size_t(ty) * L::BW + 2 * i2 + L::XO;
+        const unsigned char *sf = reinterpret_cast<const unsigned char *>(s_f) + size_t(st) * L::stage_bytes;
 #pragma unroll
         for (int q = 0; q < QQ; ++q) {
-            const S *e = reinterpret_cast<const S *>(reinterpret_cast<const unsigned char *>(sf) +
-                                                     size_t(q) * L::box_stride) -
-                         kCX[q];
+            // node xa pulls xa - c_x: element 2 i2 - c_x + shift of its row
+            const S *e = reinterpret_cast<const S *>(sf + L::box_off(q)) + ty * L::bw(q) + 2 * i2 - kCX[q] +
+                         L::shift(q);
             const V2 raw = kCX[q] == 0 ? PairStore<S>::template load<true>(e) : PairStore<S>::template load<false>(e);
             // populations as f' = f - w: FP32 stores f', 16-bit storage f'/w
             pop[q] = PairStore<S>::kScaled ? raw * V2(static_cast<float>(weight<QQ>(q))) : raw;
@@ -590,14 +593,15 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
 
 template <int QQ, bool JET, class S>
 __global__ void __launch_bounds__(NT2, PairOccupancy<QQ, S>::value)
-    k_collide_pair(const Params<float> p, const StepBuffers<S, float> b, const __grid_constant__ CUtensorMap fmap,
-                   const __grid_constant__ CUtensorMap phimap) {
+    k_collide_pair(const Params<float> p, const StepBuffers<S, float> b, const __grid_constant__ CUtensorMap fmapn,
+                   const __grid_constant__ CUtensorMap fmapw, const __grid_constant__ CUtensorMap phimap) {
     extern __shared__ __align__(128) unsigned char smem[];
     tma_pipeline_init<QQ, S, PairLayout<QQ, S>>(smem);
     const int zb = 1 + blockIdx.z * p.zchunk;
     const int ze = min(zb + p.zchunk, int(p.nz) - 1);
     uint32_t seq = 0;
-    collide_tile_pair<QQ, JET, S>(p, b, &fmap, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb, ze, smem, seq);
+    collide_tile_pair<QQ, JET, S>(p, b, &fmapn, &fmapw, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb, ze,
+                                  smem, seq);
 }
 
 }  // namespace pflbm

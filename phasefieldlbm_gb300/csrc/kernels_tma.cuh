@@ -5,10 +5,11 @@
 // a chunk of z planes, but the populations of a plane are brought into
 // shared memory by the Tensor Memory Accelerator up to NS-1 planes ahead of
 // use (NS = 2..4 stages, as many as keep the CollideOccupancy CTAs resident):
-//   * f: one 4D tensor map (x, y, z, q). For plane z and direction q the CTA
-//     needs the source tile shifted by -c_q; it loads one box per direction,
-//     (32 + 2*XO) x 8 wide, whose x origin x0 - XO is 16-byte aligned, at
-//     y0 - cy_q and z - cz_q; the thread reads element tx + XO - cx_q.
+//   * f: two 4D tensor maps (x, y, z, q) that differ in box width. For plane
+//     z and direction q the CTA needs the source tile shifted by -c_q; it
+//     loads one box per direction at y0 - cy_q and z - cz_q: 32 x 8 at x0
+//     when c_x = 0, else (32 + XU) x 8 with XU the 16-byte unit of x, at
+//     x0 - XU (c_x = +1) or x0 (c_x = -1); see TmaPlan.
 //   * phi: one 3D tensor map, box 40 x 12 (tile + halo 2) at (x0-4, y0-2),
 //     two planes ahead of the plane the stage carries, into a ring of NS+2
 //     slots.
@@ -61,23 +62,40 @@ __device__ __forceinline__ void normal_pair(const Elem &e, bool va, bool vb, V2 
 __host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~size_t(127); }
 
 // Shared-memory plan of the TMA collide kernel with NS population stages
-// (planes in flight = NS - 1 ahead of the one being collided).
+// (planes in flight = NS - 1 ahead of the one being collided). Direction q
+// of plane z comes as one box of TY rows: TX wide at x0 when c_x = 0 (no x
+// halo is read), TX + XU wide otherwise, where XU is the 16-byte alignment
+// unit of the x coordinate, starting at x0 - XU for c_x = +1 (halo column
+// x0 - 1) and at x0 for c_x = -1 (halo column x0 + TX).
 template <int QQ, class S, int NS>
 struct TmaPlan {
     using T = typename Store<S>::T;
     static constexpr int kStages = NS;
-    static constexpr int XO = sizeof(S) == 2 ? 8 : 4;  // x origin offset: 16-byte aligned coordinate
-    static constexpr int BW = TX + 2 * XO;             // f box width
-    static constexpr int PXO = 4;                      // phi is FP32 or FP64
-    static constexpr int PBW = TX + 2 * PXO;           // 40
-    static constexpr int PBH = TY + 4;                 // 12
-    static constexpr int kPhiSlots = NS + 2;           // phi planes z .. z + NS + 1
-    // bytes the TMA unit writes per box / phi plane
-    static constexpr size_t box_bytes = size_t(TY) * BW * sizeof(S);
+    static constexpr int XU = 16 / int(sizeof(S));  // elements per 16 bytes
+    static constexpr int BWN = TX;                  // box width, c_x = 0
+    static constexpr int BWW = TX + XU;             // box width, c_x != 0
+    static constexpr int PXO = 4;                   // phi is FP32 or FP64
+    static constexpr int PBW = TX + 2 * PXO;        // 40
+    static constexpr int PBH = TY + 4;              // 12
+    static constexpr int kPhiSlots = NS + 2;        // phi planes z .. z + NS + 1
+    // per direction: box width, x origin shift (box starts at x0 - shift),
+    // bytes and 128-byte aligned offset inside a stage
+    static constexpr int bw(int q) { return detail::dir_c(0, q) == 0 ? BWN : BWW; }
+    static constexpr int shift(int q) { return detail::dir_c(0, q) > 0 ? XU : 0; }
+    static constexpr size_t box_bytes(int q) { return size_t(TY) * bw(q) * sizeof(S); }
+    static constexpr size_t box_off(int q) {
+        size_t o = 0;
+        for (int k = 0; k < q; ++k) o += align128(box_bytes(k));
+        return o;
+    }
+    static constexpr size_t f_bytes() {
+        size_t o = 0;
+        for (int k = 0; k < QQ; ++k) o += box_bytes(k);
+        return o;
+    }
     static constexpr size_t phi_plane_bytes = size_t(PBH) * PBW * sizeof(T);
     // shared-memory strides: every TMA destination starts on a 128-byte boundary
-    static constexpr size_t box_stride = align128(box_bytes);
-    static constexpr size_t stage_bytes = size_t(QQ) * box_stride;
+    static constexpr size_t stage_bytes = box_off(QQ);
     static constexpr size_t phi_slot_bytes = align128(phi_plane_bytes);
     static constexpr size_t off_f = 0;
     static constexpr size_t off_phi = align128(NS * stage_bytes);
@@ -89,10 +107,11 @@ struct TmaPlan {
     static constexpr size_t ind_bytes = size_t(3) * TY * NX_ * sizeof(T);
     static constexpr size_t off_bar = align128(off_ind + ind_bytes);
     static constexpr size_t total = off_bar + 128;  // NS mbarriers + the abort flag
-    static constexpr uint32_t tx_bytes = uint32_t(QQ * box_bytes + phi_plane_bytes);
-    static_assert(box_stride % 128 == 0 && phi_slot_bytes % 128 == 0 && off_phi % 128 == 0, "TMA smem alignment");
-    static_assert((BW * sizeof(S)) % 16 == 0 && (PBW * sizeof(T)) % 16 == 0, "TMA inner box extent");
-    static_assert(BW <= 256 && PBW <= 256 && TY <= 256 && PBH <= 256, "TMA box dimension limit");
+    static constexpr uint32_t tx_bytes = uint32_t(f_bytes() + phi_plane_bytes);
+    static_assert(stage_bytes % 128 == 0 && phi_slot_bytes % 128 == 0 && off_phi % 128 == 0, "TMA smem alignment");
+    static_assert((BWN * sizeof(S)) % 16 == 0 && (BWW * sizeof(S)) % 16 == 0 && (PBW * sizeof(T)) % 16 == 0,
+                  "TMA inner box extent");
+    static_assert(BWW <= 256 && PBW <= 256 && TY <= 256 && PBH <= 256, "TMA box dimension limit");
     static_assert(NS >= 2 && NS * 8 + 4 <= 128, "mbarrier area");
 };
 
@@ -152,9 +171,9 @@ __device__ __forceinline__ void tma_pipeline_init(unsigned char *smem) {
 template <int QQ, bool JET, class S, int MODE>
 __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>::T> &p,
                                                  const StepBuffers<S, typename Store<S>::T> &b,
-                                                 const CUtensorMap *fmap_p, const CUtensorMap *phimap_p, int x0,
-                                                 int y0, int zb, int ze, unsigned char *smem, uint32_t &seq,
-                                                 float *s_mlp = nullptr) {
+                                                 const CUtensorMap *fmapn_p, const CUtensorMap *fmapw_p,
+                                                 const CUtensorMap *phimap_p, int x0, int y0, int zb, int ze,
+                                                 unsigned char *smem, uint32_t &seq, float *s_mlp = nullptr) {
     using T = typename Store<S>::T;
     using L = TmaLayout<QQ, S>;
     S *s_f = reinterpret_cast<S *>(smem + L::off_f);
@@ -187,12 +206,14 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         unsigned char *dst = reinterpret_cast<unsigned char *>(s_f) + size_t(stage) * L::stage_bytes;
 #pragma unroll
         for (int q = 0; q < QQ; ++q)
-            tma_load_4d(dst + size_t(q) * L::box_stride, fmap_p, &bar[stage], x0 - L::XO, y0 - kCY[q], zf - kCZ[q], q);
+            tma_load_4d(dst + L::box_off(q), kCX[q] == 0 ? fmapn_p : fmapw_p, &bar[stage], x0 - L::shift(q),
+                        y0 - kCY[q], zf - kCZ[q], q);
         tma_load_3d(&phi_at(pslot(zf + 2), 0, 0), phimap_p, &bar[stage], x0 - L::PXO, y0 - 2, zf + 2);
     };
 
     if (tid == 0) {
-        tma_prefetch_desc(fmap_p);
+        tma_prefetch_desc(fmapn_p);
+        tma_prefetch_desc(fmapw_p);
         tma_prefetch_desc(phimap_p);
     }
 
@@ -294,17 +315,17 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         const T phi = phi_at(pslot(z), ty + 2, tx + L::PXO);
 
         T pop[QQ];
-        const unsigned char *sf = reinterpret_cast<const unsigned char *>(s_f) + size_t(st) * L::stage_bytes +
-                                  (size_t(ty) * L::BW + tx + L::XO) * sizeof(S);
+        const unsigned char *sf = reinterpret_cast<const unsigned char *>(s_f) + size_t(st) * L::stage_bytes;
         if (kWarpWide && !col) {
 #pragma unroll
             for (int q = 0; q < QQ; ++q) pop[q] = T(0);  // placeholder node of the warp-wide network
         } else {
+            // node x = x0 + tx pulls x - c_x: element tx - c_x + shift of its row
 #pragma unroll
             for (int q = 0; q < QQ; ++q)
-                pop[q] = Store<S>::widen(
-                    *reinterpret_cast<const S *>(sf + size_t(q) * L::box_stride - kCX[q] * int(sizeof(S))),
-                    static_cast<T>(weight<QQ>(q)));
+                pop[q] = Store<S>::widen(reinterpret_cast<const S *>(sf + L::box_off(q))[ty * L::bw(q) + tx - kCX[q] +
+                                                                                          L::shift(q)],
+                                         static_cast<T>(weight<QQ>(q)));
         }
         collide_node<QQ, JET, S, MODE>(p, b, x, y, z, t, pop, phi, n_x, n_y, n_z, ind, curvature, s_mlp, col);
     }
@@ -315,7 +336,8 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
 template <int QQ, bool JET, class S, int MODE>
 __global__ void __launch_bounds__(NT, CollideOccupancy<QQ, S>::value)
     k_collide_tma(const Params<typename Store<S>::T> p, const StepBuffers<S, typename Store<S>::T> b,
-                  const __grid_constant__ CUtensorMap fmap, const __grid_constant__ CUtensorMap phimap) {
+                  const __grid_constant__ CUtensorMap fmapn, const __grid_constant__ CUtensorMap fmapw,
+                  const __grid_constant__ CUtensorMap phimap) {
     extern __shared__ __align__(128) unsigned char smem[];
     float *s_mlp = nullptr;
     if constexpr (mode_closure(MODE)) {
@@ -333,8 +355,8 @@ __global__ void __launch_bounds__(NT, CollideOccupancy<QQ, S>::value)
     const int zb = 1 + blockIdx.z * p.zchunk;
     const int ze = min(zb + p.zchunk, int(p.nz) - 1);
     uint32_t seq = 0;
-    collide_tile_tma<QQ, JET, S, MODE>(p, b, &fmap, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb, ze, smem,
-                                       seq, s_mlp);
+    collide_tile_tma<QQ, JET, S, MODE>(p, b, &fmapn, &fmapw, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb,
+                                       ze, smem, seq, s_mlp);
 }
 
 }  // namespace pflbm
