@@ -173,8 +173,8 @@ def cpu_oracle_mlups(cfg, steps: int, warm: int = 1) -> tuple[float, float, int]
 # 128x128x512 workload by the number of interior planes (510 / 126); see
 # profiles/k_collide_tma_jet_d3q27_fp32_128x128x128.md and ..._d3q19_....md.
 NCU_COLLIDE_TRAFFIC = {
-    "jet_d3q27": (250.133248e6 + 199.088384e6) * 510 / 126,
-    "jet_d3q19": (179.500544e6 + 132.328704e6) * 510 / 126,
+    "jet_d3q27": (249.849088e6 + 195.644672e6) * 510 / 126,
+    "jet_d3q19": (179.140864e6 + 127.638528e6) * 510 / 126,
 }
 
 
