@@ -16,6 +16,8 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <new>
+#include <system_error>
 #include <string>
 #include <sys/stat.h>
 #include <thread>
@@ -277,15 +279,18 @@ int copy_out(pflbm_sim *s, const void *dev, size_t n, void *host, bool as_double
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy D2H");
         return PFLBM_OK;
     }
-    std::vector<unsigned char> tmp(n * rb);
-    e = cudaMemcpy(tmp.data(), dev, n * rb, cudaMemcpyDeviceToHost);
+    // conversion buffer: allocated without exceptions, which must not
+    // cross the C ABI
+    std::unique_ptr<unsigned char[]> tmp(new (std::nothrow) unsigned char[n * rb]);
+    if (!tmp) return fail(PFLBM_ERR_OUT_OF_MEMORY, "host conversion buffer");
+    e = cudaMemcpy(tmp.get(), dev, n * rb, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy D2H");
     if (rb == 4) {
-        const float *src = reinterpret_cast<const float *>(tmp.data());
+        const float *src = reinterpret_cast<const float *>(tmp.get());
         double *dst = static_cast<double *>(host);
         for (size_t i = 0; i < n; ++i) dst[i] = src[i];
     } else {
-        const double *src = reinterpret_cast<const double *>(tmp.data());
+        const double *src = reinterpret_cast<const double *>(tmp.get());
         float *dst = static_cast<float *>(host);
         for (size_t i = 0; i < n; ++i) dst[i] = float(src[i]);
     }
@@ -584,8 +589,10 @@ int pflbm_set_initial_field(pflbm_sim *s, int32_t id, const float *src, size_t b
     if (rb == 4) {
         e = cudaMemcpy(dst, src, N * 4, cudaMemcpyHostToDevice);
     } else {
-        std::vector<double> tmp(src, src + N);
-        e = cudaMemcpy(dst, tmp.data(), N * 8, cudaMemcpyHostToDevice);
+        std::unique_ptr<double[]> tmp(new (std::nothrow) double[N]);
+        if (!tmp) return fail(PFLBM_ERR_OUT_OF_MEMORY, "host conversion buffer");
+        for (uint64_t i = 0; i < N; ++i) tmp[i] = src[i];
+        e = cudaMemcpy(dst, tmp.get(), N * 8, cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy H2D");
     s->distros_dirty = true;
@@ -823,12 +830,20 @@ int pflbm_write_output_async(pflbm_sim *s, const char *dir, const int32_t *ids, 
     }
     const std::string suffix = step6(s->step > 0 ? s->step - 1 : 0);
     const uint32_t nx = s->hp.nx, ny = s->hp.ny, nz = s->hp.nz;
-    s->writer = std::thread([s, d, suffix, names, data, N, nx, ny, nz]() {
+    auto job = [s, d, suffix, names, data, N, nx, ny, nz]() {
         std::string err;
         const int r = write_step_files(d, suffix, names, data, N, nx, ny, nz, err);
         s->writer_err = err;
         s->writer_rc = r;
-    });
+    };
+    try {
+        s->writer = std::thread(job);
+    } catch (const std::system_error &) {
+        // no thread could be started: write in the calling thread instead
+        // (exceptions must not cross the C ABI)
+        job();
+        return join_writer(s);
+    }
     return PFLBM_OK;
 }
 
@@ -853,26 +868,30 @@ struct CkptHeader {
 };
 
 int write_blob(std::ofstream &o, const void *dev, uint64_t bytes) {
-    std::vector<char> h(1 << 26);
-    for (uint64_t off = 0; off < bytes; off += h.size()) {
-        const size_t n = size_t(std::min<uint64_t>(h.size(), bytes - off));
-        cudaError_t e = cudaMemcpy(h.data(), static_cast<const char *>(dev) + off, n, cudaMemcpyDeviceToHost);
+    constexpr size_t kChunkBytes = size_t(1) << 26;
+    std::unique_ptr<char[]> h(new (std::nothrow) char[kChunkBytes]);
+    if (!h) return fail(PFLBM_ERR_OUT_OF_MEMORY, "checkpoint staging buffer");
+    for (uint64_t off = 0; off < bytes; off += kChunkBytes) {
+        const size_t n = size_t(std::min<uint64_t>(kChunkBytes, bytes - off));
+        cudaError_t e = cudaMemcpy(h.get(), static_cast<const char *>(dev) + off, n, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "checkpoint D2H");
-        o.write(h.data(), std::streamsize(n));
+        o.write(h.get(), std::streamsize(n));
         if (!o) return fail(PFLBM_ERR_IO, "checkpoint write failed");
     }
     return PFLBM_OK;
 }
 
 int read_blob(std::ifstream &in, void *dev0, void *dev1, uint64_t bytes) {
-    std::vector<char> h(1 << 26);
-    for (uint64_t off = 0; off < bytes; off += h.size()) {
-        const size_t n = size_t(std::min<uint64_t>(h.size(), bytes - off));
-        in.read(h.data(), std::streamsize(n));
+    constexpr size_t kChunkBytes = size_t(1) << 26;
+    std::unique_ptr<char[]> h(new (std::nothrow) char[kChunkBytes]);
+    if (!h) return fail(PFLBM_ERR_OUT_OF_MEMORY, "checkpoint staging buffer");
+    for (uint64_t off = 0; off < bytes; off += kChunkBytes) {
+        const size_t n = size_t(std::min<uint64_t>(kChunkBytes, bytes - off));
+        in.read(h.get(), std::streamsize(n));
         if (!in) return fail(PFLBM_ERR_IO, "checkpoint truncated");
         for (void *d : {dev0, dev1}) {
             if (!d) continue;
-            cudaError_t e = cudaMemcpy(static_cast<char *>(d) + off, h.data(), n, cudaMemcpyHostToDevice);
+            cudaError_t e = cudaMemcpy(static_cast<char *>(d) + off, h.get(), n, cudaMemcpyHostToDevice);
             if (e != cudaSuccess) return cuda_fail(e, "checkpoint H2D");
         }
     }

@@ -27,6 +27,7 @@
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -412,7 +413,8 @@ int pflbm_closure_create(int32_t device, uint64_t max_samples, pflbm_closure **o
         return fail(PFLBM_ERR_CUDA, "no CUDA device");
     }
     if (device < 0 || device >= ndev) return fail(PFLBM_ERR_INVALID_ARG, "device out of range");
-    std::unique_ptr<pflbm_closure> c(new pflbm_closure());
+    std::unique_ptr<pflbm_closure> c(new (std::nothrow) pflbm_closure());
+    if (!c) return fail(PFLBM_ERR_OUT_OF_MEMORY, "closure handle");
     c->device = device;
     cudaSetDevice(device);
     c->cap = max_samples;
