@@ -52,6 +52,11 @@ EXPORTED_SYMBOLS = [
     "pflbm_ensemble_create", "pflbm_ensemble_init", "pflbm_ensemble_step", "pflbm_ensemble_step_profiled",
     "pflbm_ensemble_get_field", "pflbm_ensemble_reduce", "pflbm_ensemble_set_tuning", "pflbm_ensemble_autotune",
     "pflbm_ensemble_info", "pflbm_ensemble_destroy",
+    "pflbm_reduce_fields_noalloc", "pflbm_write_output_async", "pflbm_set_watchdog",
+    "pflbm_closure_create", "pflbm_closure_add_snapshot", "pflbm_closure_num_samples", "pflbm_closure_get_samples",
+    "pflbm_closure_set_samples", "pflbm_closure_init_params", "pflbm_closure_get_blob", "pflbm_closure_set_blob",
+    "pflbm_closure_gradient", "pflbm_closure_train", "pflbm_closure_loss", "pflbm_closure_destroy",
+    "pflbm_set_closure",
 ]
 
 
