@@ -17,6 +17,10 @@ if [ "$VELOCITY_SET" != "D3Q19" ] && [ "$VELOCITY_SET" != "D3Q27" ]; then
     echo "Invalid VELOCITY_SET. Use 'D3Q19' or 'D3Q27'."
     exit 1
 fi
+if ! [[ "$ID" =~ ^[A-Za-z0-9_-]+$ ]]; then
+    echo "Invalid ID '$ID': use letters, digits, '_' or '-'."
+    exit 1
+fi
 BASE_DIR="$(cd -- "$(dirname -- "${BASH_SOURCE[0]}")" &>/dev/null && pwd)"
 CC=${GPU_ARCH:-103}
 OUTPUT_DIR="${BASE_DIR}/bin/${FLOW_CASE}/${VELOCITY_SET}"

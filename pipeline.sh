@@ -14,6 +14,13 @@ if [ -z "$FLOW_CASE" ] || [ -z "$VELOCITY_SET" ] || [ -z "$ID" ]; then
     echo "Example: ./pipeline.sh JET D3Q19 000"
     exit 1
 fi
+case "$FLOW_CASE" in JET|DROPLET) ;; *) echo "Invalid flow_case. Use 'JET' or 'DROPLET'."; exit 1 ;; esac
+case "$VELOCITY_SET" in D3Q19|D3Q27) ;; *) echo "Invalid velocity_set. Use 'D3Q19' or 'D3Q27'."; exit 1 ;; esac
+# the id names a directory that is emptied below: letters, digits, '_' and '-' only
+if ! [[ "$ID" =~ ^[A-Za-z0-9_-]+$ ]]; then
+    echo "Invalid id '$ID': use letters, digits, '_' or '-'."
+    exit 1
+fi
 shift 3
 BASE_DIR="$(cd -- "$(dirname -- "${BASH_SOURCE[0]}")" &>/dev/null && pwd)"
 SIMULATION_DIR="${BASE_DIR}/bin/${FLOW_CASE}/${VELOCITY_SET}/${ID}"
