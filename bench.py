@@ -184,15 +184,48 @@ def traffic_for(workload: str):
 
 
 # ---------------------------------------------------------------- arms
-def workload_config(args):
-    """The bench workload; --nz shortens the jet for profiling captures."""
+def workload_config(args, base=None):
+    """The bench workload; --nz shortens the jet for profiling captures.
+    `base` supplies the reference configuration the preset starts from (the
+    reference arm passes the oracle's own, so that it loads no library)."""
     import phasefieldlbm_gb300 as pf
 
     st = {"fp32": pf.STORAGE_FP32, "fp16": pf.STORAGE_FP16, "bf16": pf.STORAGE_BF16, "fp64": pf.STORAGE_FP64}
     kw = {"storage": st[args.storage]}
     if args.nz:
         kw["nz"] = args.nz
-    return pf.preset(args.workload, **kw)
+    return pf.preset(args.workload, base=base, **kw)
+
+
+def reference_build_mlups(workload: str, steps: int, nz: int = 0):
+    """GPU baseline: the reference's own CUDA build (its src/main.cu compiled
+    for sm_103a with the benchmark preset's physics patched in, run by
+    oracle/ref_runner with src/main.cu's launch sequence and per-step sync),
+    timed on the host wall clock around the step loop as src/main.cu:199-205
+    does. None when the cubins were not built (they come from the reference
+    sources, present only where the repository was prepared)."""
+    from oracle import ref_build
+
+    name = {"jet_d3q27": "jet_d3q27_bench", "jet_d3q19": "jet_d3q19_bench"}.get(workload)
+    entry = ref_build.manifest().get(name) if name else None
+    if not entry or nz or not (ref_build.OUT / entry["cubin"]).exists():
+        return None
+    try:
+        exe = ref_build.build_runner()
+        nx, ny, nzz = entry["dims"]
+        r = subprocess.run([str(exe), str(ref_build.OUT / entry["cubin"]), entry["case"], str(entry["q"]), str(nx),
+                            str(ny), str(nzz), str(entry["fp16"]), str(steps), "-", "time"],
+                           capture_output=True, text=True, timeout=300)
+        if r.returncode != 0:
+            return {"value": None, "error": (r.stderr or r.stdout)[-200:]}
+        line = json.loads(r.stdout.strip().splitlines()[-1])
+    except Exception as ex:  # a baseline leg: report why it is missing
+        return {"value": None, "error": str(ex)[:200]}
+    return {"value": round(line["ref_mlups"], 2), "unit": "MLUPS", "kind": "reference_cuda_build",
+            "steps": steps, "seconds": round(line["seconds"], 4),
+            "sample": f"the reference's own kernels (src/main.cu built for sm_103a, FP32 f, preset physics patched "
+                      f"in: gamma 0.05, uniform u_z noise seed 12345) on {nx}x{ny}x{nzz}, {steps} steps of its "
+                      "5-kernel graph + inflow + outflow + stream sync, host wall clock (src/main.cu:199-205)"}
 
 
 def run_gpu(args, ranks: Ranks) -> dict:
@@ -326,6 +359,11 @@ def run_gpu(args, ranks: Ranks) -> dict:
                "sample": f"{csteps} time steps of the full {cfg.nx}x{cfg.ny}x{cfg.nz} D3Q{q} jet (FP32) after 1 warm-up "
                          f"step, OpenMP transcription of the reference kernels, {dt:.1f} s"}
 
+    # the reference's own CUDA build on the same GPU and workload (rank 0, N = 1)
+    gpu_base = None
+    if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
+        gpu_base = reference_build_mlups(args.workload, 1000, args.nz)
+
     return {
         "metric": "MLUPS", "value": round(value, 2), "unit": "MLUPS", "n_gpus": ranks.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3 / args.steps, 3),
@@ -336,7 +374,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
                    "preset": args.workload, "nodes": N, "lattice_steps_per_step": inner,
                    "l2": "inputs larger than L2 (f ping-pong 2x{:.0f} MB)".format(q * s_f * N / 1e6),
                    "parallelism": f"replicas x{ranks.world}"},
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roofline, "cpu_baseline": cpu, "gpu_baseline": gpu_base, "e2e": e2e,
         "gpu_launches": 2 * lattice_steps, "clocks": clk, "diverged": diverged, "tma": tma,
         "variants": variants,
     }
@@ -345,10 +383,11 @@ def run_gpu(args, ranks: Ranks) -> dict:
 def run_reference(args, ranks: Ranks) -> dict | None:
     if ranks.rank != 0:
         return None
-    import phasefieldlbm_gb300 as pf
     from oracle import pyoracle
 
-    cfg = workload_config(args)
+    # the oracle's own restatement of src/constants.cuh: this arm loads the
+    # oracle library only, never libpflbm
+    cfg = workload_config(args, base=pyoracle.config_reference)
     o = pyoracle.OracleSim(cfg)
     o.step(args.warmup)
     t0 = time.perf_counter()

@@ -215,9 +215,11 @@ int pflbm_reduce(pflbm_sim *sim, pflbm_diag *out);
  * on a device share that array: calls whose kernels overlap on the GPU (on
  * different streams) race and must be serialised by the caller. Each call
  * writes every row it reads, so no earlier call's contents leak into a result.
- * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. */
+ * The first call in each CUDA context (the module, and so the array, is
+ * loaded per context) looks up the array's device address with
+ * cudaGetSymbolAddress, with that context's device current, and caches it
+ * under the context's unique id; make that first call before any stream
+ * capture. A device reset or a new context costs one more lookup. */
 #define PFLBM_NOALLOC_MAX_PLANES 4096
 int pflbm_reduce_fields_noalloc(const float *rho, const float *ux, const float *uy, const float *uz,
                                 const float *phi, int32_t nx, int32_t ny, int32_t nz, void *stream,

@@ -230,7 +230,7 @@ class Preset:
     description: str
 
 
-def preset(name: str, **overrides) -> Config:
+def preset(name: str, base=None, **overrides) -> Config:
     """Configurations of the benchmark workloads (seeded synthetic cases).
 
     droplet64        static droplet, D3Q19, 64^3 periodic, R=16, tau=0.6,
@@ -241,18 +241,23 @@ def preset(name: str, **overrides) -> Config:
     jet_precision    D3Q19 256x256x1024, D=32
     jet_closure      D3Q19 128x128x512, D=16, Re=10000
     jet_closure_fine the same jet on the 2x finer grid: 256x256x1024, D=32
+
+    `base(flow_case, velocity_set) -> Config` supplies the reference's
+    compile-time configuration the preset starts from; by default the
+    library's pflbm_config_reference. A caller that must not load the
+    library passes another restatement of src/constants.cuh:80-141.
     """
-    lib = load_library()
-    c = Config()
+    if base is None:
+        base = config_reference
     if name == "droplet64":
-        _check(lib, lib.pflbm_config_reference(ctypes.byref(c), CASE_DROPLET, VS_D3Q19))
+        c = base(CASE_DROPLET, VS_D3Q19)
         c.nx = c.ny = c.nz = 64
         c.radius, c.diam = 16, 32
         c.tau, c.sigma, c.gamma = 0.6, 0.01, 0.05
         c.droplet_x_stretch = 1.0
     elif name in ("jet_d3q27", "jet_d3q19", "jet_precision", "jet_closure", "jet_closure_fine"):
         vs = VS_D3Q27 if name == "jet_d3q27" else VS_D3Q19
-        _check(lib, lib.pflbm_config_reference(ctypes.byref(c), CASE_JET, vs))
+        c = base(CASE_JET, vs)
         if name in ("jet_precision", "jet_closure_fine"):
             c.nx, c.ny, c.nz, c.diam = 256, 256, 1024, 32
         else:

@@ -20,7 +20,7 @@ LIB = BUILD / "libpflbm.so"
 DRIVER = BUILD / "pflbm_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
+NVCC_FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 SOURCES = ["api.cu", "engine_fp32.cu", "engine_fp64.cu", "engine_fp16.cu", "engine_bf16.cu", "ensemble.cu", "noalloc.cu", "closure.cu"]
 HOST_SOURCES = ["driver_main.cpp"]
 
@@ -79,7 +79,7 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
     # the drop-in driver executable (host C++ over the C ABI)
-    cmd = ["g++", "-O2", "-std=c++17", str(CSRC / "driver_main.cpp"), "-o", str(DRIVER), f"-L{BUILD}", "-lpflbm",
+    cmd = ["g++", "-O2", "-std=c++20", str(CSRC / "driver_main.cpp"), "-o", str(DRIVER), f"-L{BUILD}", "-lpflbm",
            "-Wl,-rpath,$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -91,22 +91,22 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
 CHECKED = BUILD / "checked"
 
 
-def build_checked(jobs: int | None = None) -> Path:
-    """A test build of the library with -DPFLBM_CHECK_BOUNDS: every guarded
-    global store of the step kernels checks its index and reports a miss in
-    the device error word instead of writing (see PFLBM_GUARD). Returns the
-    path of _build/checked/libpflbm.so (rebuilt when a source is newer)."""
-    lib = CHECKED / "libpflbm.so"
-    stamp = CHECKED / ".arch"
+def build_variant(name: str, defines: list[str], jobs: int | None = None) -> Path:
+    """A test build of the library with extra preprocessor definitions, in
+    _build/<name>/libpflbm.so (rebuilt when a source is newer). Test builds
+    are loaded only by the tests, beside the shipped library."""
+    out = BUILD / name
+    lib = out / "libpflbm.so"
+    stamp = out / ".arch"
     if (lib.exists() and stamp.exists() and stamp.read_text().strip() == platform.machine()
             and all(p.stat().st_mtime <= lib.stat().st_mtime for p in _deps())):
         return lib
-    CHECKED.mkdir(parents=True, exist_ok=True)
+    out.mkdir(parents=True, exist_ok=True)
     exe = nvcc()
 
     def compile_one(src: str) -> Path:
-        obj = CHECKED / (Path(src).stem + ".o")
-        cmd = [exe, *ARCH, *NVCC_FLAGS, "-DPFLBM_CHECK_BOUNDS", "-c", str(CSRC / src), "-o", str(obj)]
+        obj = out / (Path(src).stem + ".o")
+        cmd = [exe, *ARCH, *NVCC_FLAGS, *defines, "-c", str(CSRC / src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
@@ -122,6 +122,22 @@ def build_checked(jobs: int | None = None) -> Path:
     os.replace(tmp, lib)
     stamp.write_text(platform.machine())
     return lib
+
+
+def build_checked(jobs: int | None = None) -> Path:
+    """A test build of the library with -DPFLBM_CHECK_BOUNDS: every guarded
+    global store of the step kernels checks its index and reports a miss in
+    the device error word instead of writing (see PFLBM_GUARD). Returns the
+    path of _build/checked/libpflbm.so (rebuilt when a source is newer)."""
+    return build_variant("checked", ["-DPFLBM_CHECK_BOUNDS"], jobs)
+
+
+def build_dead_wait(jobs: int | None = None) -> Path:
+    """A test build with -DPFLBM_TEST_DEAD_WAIT: the collide pipelines' first
+    wait of every plane polls an mbarrier that nothing arrives on, with a
+    short limit, so that the bounded wait runs out and the kernel reports
+    through the device error word and returns (_build/deadwait/libpflbm.so)."""
+    return build_variant("deadwait", ["-DPFLBM_TEST_DEAD_WAIT"], jobs)
 
 
 if __name__ == "__main__":

@@ -798,8 +798,8 @@ int pflbm_set_closure(pflbm_sim *s, const float *blob, float strength) {
 }
 
 
-int pflbm_write_output_async(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
-    NvtxRange nvtx_("pflbm_write_output");
+namespace {
+int write_output_async_impl(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
     if (!s || !dir || (!ids && n > 0) || n < 0) return fail(PFLBM_ERR_INVALID_ARG, "bad argument");
     for (int i = 0; i < n; ++i)
         if (ids[i] < 0 || ids[i] >= PFLBM_FIELD_COUNT) return fail(PFLBM_ERR_INVALID_ARG, "bad field id");
@@ -819,32 +819,49 @@ int pflbm_write_output_async(pflbm_sim *s, const char *dir, const int32_t *ids, 
         s->pinned.push_back(p);
     }
     // device -> page-locked host copies now (the analysis of the last step
-    // runs once); the file writes overlap with whatever the caller does next
-    std::vector<std::string> names;
-    std::vector<const float *> data;
-    for (int i = 0; i < n; ++i) {
-        rc = pflbm_get_field(s, ids[i], s->pinned[i], N * sizeof(float));
-        if (rc) return rc;
-        names.push_back(kFieldNames[ids[i]]);
-        data.push_back(s->pinned[i]);
-    }
-    const std::string suffix = step6(s->step > 0 ? s->step - 1 : 0);
-    const uint32_t nx = s->hp.nx, ny = s->hp.ny, nz = s->hp.nz;
-    auto job = [s, d, suffix, names, data, N, nx, ny, nz]() {
-        std::string err;
-        const int r = write_step_files(d, suffix, names, data, N, nx, ny, nz, err);
-        s->writer_err = err;
-        s->writer_rc = r;
-    };
+    // runs once); the file writes overlap with whatever the caller does next.
+    // No exception may cross the C ABI: a failed host allocation anywhere
+    // below (vectors, strings, the copy of the job into the thread) becomes
+    // PFLBM_ERR_OUT_OF_MEMORY.
     try {
-        s->writer = std::thread(job);
-    } catch (const std::system_error &) {
-        // no thread could be started: write in the calling thread instead
-        // (exceptions must not cross the C ABI)
-        job();
-        return join_writer(s);
+        std::vector<std::string> names;
+        std::vector<const float *> data;
+        for (int i = 0; i < n; ++i) {
+            rc = pflbm_get_field(s, ids[i], s->pinned[i], N * sizeof(float));
+            if (rc) return rc;
+            names.push_back(kFieldNames[ids[i]]);
+            data.push_back(s->pinned[i]);
+        }
+        const std::string suffix = step6(s->step > 0 ? s->step - 1 : 0);
+        const uint32_t nx = s->hp.nx, ny = s->hp.ny, nz = s->hp.nz;
+        auto job = [s, d, suffix, names, data, N, nx, ny, nz]() {
+            std::string err;
+            const int r = write_step_files(d, suffix, names, data, N, nx, ny, nz, err);
+            s->writer_err = err;
+            s->writer_rc = r;
+        };
+        try {
+            s->writer = std::thread(job);  // a copy: `job` stays whole for the fallback
+        } catch (const std::system_error &) {
+            // no thread could be started: write in the calling thread instead
+            job();
+            return join_writer(s);
+        }
+    } catch (...) {
+        return fail(PFLBM_ERR_OUT_OF_MEMORY, "host allocation failed in the output writer");
     }
     return PFLBM_OK;
+}
+}  // namespace
+
+int pflbm_write_output_async(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
+    NvtxRange nvtx_("pflbm_write_output");
+    // no exception crosses the C ABI (the path string, the staging list)
+    try {
+        return write_output_async_impl(s, dir, ids, n);
+    } catch (...) {
+        return fail(PFLBM_ERR_OUT_OF_MEMORY, "host allocation failed in the output writer");
+    }
 }
 
 int pflbm_write_output(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {

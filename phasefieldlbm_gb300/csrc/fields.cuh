@@ -8,6 +8,7 @@
 #include "boundary.cuh"
 #include "lattice.cuh"
 #include "params.cuh"
+#include "reduce.cuh"
 #include "tile.h"
 
 namespace pflbm {
@@ -157,7 +158,6 @@ __global__ void k_vorticity(const Params<T> p, const T *macro, T *vort) {
 // FP64 diagnostics: per-block partial sums over interior nodes, then a
 // single-block pass over the partials in fixed order (deterministic).
 constexpr int RED_THREADS = 256;
-constexpr int RED_FIELDS = 12;  // phi, rho, rho ux, rho uy, rho uz, max|u|, rho_in, n_in, rho_out, n_out, nonfinite, spare
 
 template <class T>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(const Params<T> p, const T *macro, double *partial) {
@@ -185,17 +185,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(const Params<T> 
         if (phi > 0.9) { acc[6] += rho; acc[7] += 1.0; }
         if (phi < 0.1) { acc[8] += rho; acc[9] += 1.0; }
     }
-    __shared__ double sh[RED_FIELDS][RED_THREADS];
-    for (int f = 0; f < RED_FIELDS; ++f) sh[f][threadIdx.x] = acc[f];
-    __syncthreads();
-    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int f = 0; f < RED_FIELDS; ++f)
-                sh[f][threadIdx.x] = (f == 5) ? fmax(sh[f][threadIdx.x], sh[f][threadIdx.x + s])
-                                              : sh[f][threadIdx.x] + sh[f][threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x < RED_FIELDS) partial[blockIdx.x * RED_FIELDS + threadIdx.x] = sh[threadIdx.x][0];
+    block_reduce_row<RED_THREADS>(acc, partial + size_t(blockIdx.x) * RED_FIELDS);
 }
 
 static __global__ void __launch_bounds__(32) k_reduce_final(const double *partial, int nblocks, double *out) {
@@ -204,7 +194,7 @@ static __global__ void __launch_bounds__(32) k_reduce_final(const double *partia
     double s = 0.0;
     for (int b = 0; b < nblocks; ++b) {
         const double v = partial[b * RED_FIELDS + f];
-        s = (f == 5) ? fmax(s, v) : s + v;
+        s = red_combine(f, s, v);
     }
     out[f] = s;
 }

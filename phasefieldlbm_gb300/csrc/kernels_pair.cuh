@@ -546,7 +546,7 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
         const uint32_t sq = seq + uint32_t(z - zb);
         const int st = int(sq % NS);
         const uint32_t par = (sq / NS) & 1;
-        if (!mbar_wait_bounded(&bar[st], par, kWaitLimit)) *s_abort = 1;
+        if (!plane_wait<L>(smem, &bar[st], par)) *s_abort = 1;
         compute_n(z + 1);
         __syncthreads();
         if (*s_abort) {

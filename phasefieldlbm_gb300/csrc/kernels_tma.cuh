@@ -106,13 +106,15 @@ struct TmaPlan {
     static constexpr size_t off_ind = align128(off_n + n_bytes);
     static constexpr size_t ind_bytes = size_t(3) * TY * NX_ * sizeof(T);
     static constexpr size_t off_bar = align128(off_ind + ind_bytes);
-    static constexpr size_t total = off_bar + 128;  // NS mbarriers + the abort flag
+    // NS mbarriers, the abort flag, and at off_bar + 64 the test build's
+    // never-arriving barrier (plane_wait)
+    static constexpr size_t total = off_bar + 128;
     static constexpr uint32_t tx_bytes = uint32_t(f_bytes() + phi_plane_bytes);
     static_assert(stage_bytes % 128 == 0 && phi_slot_bytes % 128 == 0 && off_phi % 128 == 0, "TMA smem alignment");
     static_assert((BWN * sizeof(S)) % 16 == 0 && (BWW * sizeof(S)) % 16 == 0 && (PBW * sizeof(T)) % 16 == 0,
                   "TMA inner box extent");
     static_assert(BWW <= 256 && PBW <= 256 && TY <= 256 && PBH <= 256, "TMA box dimension limit");
-    static_assert(NS >= 2 && NS * 8 + 4 <= 128, "mbarrier area");
+    static_assert(NS >= 2 && NS * 8 + 4 <= 64, "mbarrier area");
 };
 
 // Deepest pipeline (4, 3 or 2 stages) that keeps two CTAs per SM (FP32 and
@@ -158,9 +160,29 @@ __device__ __forceinline__ void tma_pipeline_init(unsigned char *smem) {
         uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
         for (int k = 0; k < L::kStages; ++k) mbar_init(&bar[k], 1);
         *reinterpret_cast<volatile int *>(smem + L::off_bar + 8 * L::kStages) = 0;
+#ifdef PFLBM_TEST_DEAD_WAIT
+        mbar_init(reinterpret_cast<uint64_t *>(smem + L::off_bar + 64), 1);
+#endif
         fence_mbar_init();
     }
     __syncthreads();
+}
+
+// The per-plane wait of the collide pipelines: phase `parity` of the stage's
+// barrier, bounded. A test build (-DPFLBM_TEST_DEAD_WAIT, never the shipped
+// library) polls instead a barrier that nothing arrives on, with a short
+// limit, so that the wait always runs out and the failure path (error word,
+// drain of the CTA's own copies at the full limit, return) is exercised.
+template <class L>
+__device__ __forceinline__ bool plane_wait(unsigned char *smem, uint64_t *bar, uint32_t parity) {
+#ifdef PFLBM_TEST_DEAD_WAIT
+    (void)bar;
+    (void)parity;
+    return mbar_wait_bounded(reinterpret_cast<uint64_t *>(smem + L::off_bar + 64), 0, 1u << 12);
+#else
+    (void)smem;
+    return mbar_wait_bounded(bar, parity, kWaitLimit);
+#endif
 }
 
 // One column tile [x0, x0+TX) x [y0, y0+TY), planes zb .. ze-1. `seq` counts
@@ -285,7 +307,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         const uint32_t sq = seq + uint32_t(z - zb);
         const int st = int(sq % NS);
         const uint32_t par = (sq / NS) & 1;
-        if (!mbar_wait_bounded(&bar[st], par, kWaitLimit)) *s_abort = 1;
+        if (!plane_wait<L>(smem, &bar[st], par)) *s_abort = 1;
         compute_n(z + 1);
         __syncthreads();
         if (*s_abort) {

@@ -14,6 +14,7 @@
 // call on a device shares it, so calls whose kernels overlap on that GPU race
 // on it; each call writes every row it later reads, so nothing has to start at
 // zero and the contents left by an earlier call are never read.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -22,22 +23,35 @@
 
 #include "../../include/pflbm.h"
 #include "engine.h"
+#include "reduce.cuh"
 
 namespace {
 
-constexpr int kFields = 12;  // phi, rho, rho ux, rho uy, rho uz, max|u|, rho_in, n_in, rho_out, n_out, nonfinite, spare
+constexpr int kFields = pflbm::RED_FIELDS;
 constexpr int kThreads = 256;
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 constexpr size_t kScratchDoubles = size_t(PFLBM_NOALLOC_MAX_PLANES) * kFields;
 constexpr size_t kScratchBytes = kScratchDoubles * sizeof(double);  // 384 KiB
 static_assert(kScratchBytes == 384 * 1024, "scratch size stated in pflbm.h");
 
 // Host code sees only a stand-in symbol; the device address comes from
-// cudaGetSymbolAddress, once per device.
+// cudaGetSymbolAddress, once per CUDA context.
 static __device__ __align__(256) double g_plane_partials[kScratchDoubles];
 
+// Device addresses of g_plane_partials, one per CUDA context that has called
+// (the module, and with it the array, is loaded per context: a device reset
+// or a caller's own non-primary context gets a new one). Keyed by the
+// context's unique id, which is never reused within a process.
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    double *ptr;
+};
 std::mutex g_setup_mutex;
-double *g_scratch[kMaxDevices] = {};
+ScratchEntry g_scratch[kMaxContexts] = {};
+int g_scratch_next = 0;  // round-robin slot for a new context
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
 
 int fail(int code, const std::string &msg) {
     pflbm::set_error(msg);
@@ -49,16 +63,51 @@ int cuda_fail(cudaError_t e, const char *what) {
     return fail(PFLBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Device address of g_plane_partials on `device` (which is current).
-int scratch_for(int device, double **out) {
+// Unique id of the current CUDA context (driver entry points through the
+// runtime, so the library needs no link against libcuda).
+int current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess && a &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess && b) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+            get_id = reinterpret_cast<CtxGetIdFn>(b);
+        } else {
+            cudaGetLastError();
+        }
+    });
+    if (!get_current || !get_id)
+        return fail(PFLBM_ERR_CUDA, "driver entry points cuCtxGetCurrent / cuCtxGetId unavailable");
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx)
+        return fail(PFLBM_ERR_CUDA, "no current CUDA context");
+    if (get_id(ctx, id) != CUDA_SUCCESS) return fail(PFLBM_ERR_CUDA, "cuCtxGetId failed");
+    return PFLBM_OK;
+}
+
+// Device address of g_plane_partials in the current context, looked up with
+// cudaGetSymbolAddress on the first call in that context and cached.
+int scratch_for_current_context(double **out) {
+    unsigned long long id = 0;
+    if (int rc = current_context_id(&id)) return rc;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch[device]) {
-        double *ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_plane_partials);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(plane partials)");
-        g_scratch[device] = ptr;
-    }
-    *out = g_scratch[device];
+    for (const ScratchEntry &en : g_scratch)
+        if (en.ptr && en.ctx_id == id) {
+            *out = en.ptr;
+            return PFLBM_OK;
+        }
+    double *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_plane_partials);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(plane partials)");
+    g_scratch[g_scratch_next] = {id, ptr};
+    g_scratch_next = (g_scratch_next + 1) % kMaxContexts;
+    *out = ptr;
     return PFLBM_OK;
 }
 
@@ -99,17 +148,7 @@ __global__ void __launch_bounds__(kThreads)
         if (f > 0.9) { acc[6] += r; acc[7] += 1.0; }
         if (f < 0.1) { acc[8] += r; acc[9] += 1.0; }
     }
-    __shared__ double sh[kFields][kThreads];
-    for (int f = 0; f < kFields; ++f) sh[f][threadIdx.x] = acc[f];
-    __syncthreads();
-    for (int s = kThreads / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int f = 0; f < kFields; ++f)
-                sh[f][threadIdx.x] = (f == 5) ? fmax(sh[f][threadIdx.x], sh[f][threadIdx.x + s])
-                                              : sh[f][threadIdx.x] + sh[f][threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x < kFields) rows[size_t(blockIdx.x) * kFields + threadIdx.x] = sh[threadIdx.x][0];
+    pflbm::block_reduce_row<kThreads>(acc, rows + size_t(blockIdx.x) * kFields);
 }
 
 // Sums the rows in plane order and writes the pflbm_diag the host entry point
@@ -121,7 +160,7 @@ __global__ void __launch_bounds__(32) k_reduce_rows(const double *__restrict__ r
         double s = 0.0;
         for (int b = 0; b < n_rows; ++b) {
             const double v = rows[size_t(b) * kFields + f];
-            s = (f == 5) ? fmax(s, v) : s + v;
+            s = pflbm::red_combine(f, s, v);
         }
         tot[f] = s;
     }
@@ -161,13 +200,12 @@ extern "C" int pflbm_reduce_fields_noalloc(const float *rho, const float *ux, co
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (device < 0 || device >= kMaxDevices) return fail(PFLBM_ERR_INVALID_ARG, "device ordinal out of range");
     const void *ptrs[6] = {rho, ux, uy, uz, phi, dev_out};
     const char *names[6] = {"rho", "ux", "uy", "uz", "phi", "dev_out"};
     for (int k = 0; k < 6; ++k)
         if (int rc = check_device_ptr(ptrs[k], device, names[k])) return rc;
     double *rows = nullptr;
-    if (int rc = scratch_for(device, &rows)) return rc;
+    if (int rc = scratch_for_current_context(&rows)) return rc;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int planes = nz - 2;
     k_reduce_planes<<<planes, kThreads, 0, s>>>(rho, ux, uy, uz, phi, nx, ny, rows);

@@ -8,12 +8,16 @@ it against the reference sources where they lie (read-only), runs it on
 seeded inputs and stores the inputs and float32 outputs. Nothing of the
 reference is copied into the repository; only the numbers are kept.
 
-    python tests/golden/gen_formulas.py [--reference /root/reference]
+    python tests/golden/gen_formulas.py [--reference <checkout>]
+
+The reference checkout defaults to PFLBM_REFERENCE_SRC, else the build
+container's copy at /root/reference.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import os
 import subprocess
 import tempfile
 from pathlib import Path
@@ -109,7 +113,7 @@ def relaxation_constants(src: Path, td: Path) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("PFLBM_REFERENCE_SRC", "/root/reference"))
     ap.add_argument("--cases", type=int, default=24)
     args = ap.parse_args()
     src = Path(args.reference) / "src"

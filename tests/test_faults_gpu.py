@@ -61,3 +61,44 @@ def test_watchdog_mass_drift(pflbm):
         with pytest.raises(pflbm.PflbmError) as e:
             s.step(100)
         assert e.value.code == 5 and "drift" in str(e.value)
+
+
+def test_bounded_tma_wait_runs_out_and_reports(pflbm):
+    """A device-side wait that runs out. The test build _build/deadwait
+    (-DPFLBM_TEST_DEAD_WAIT) makes every collide pipeline's per-plane wait
+    poll an mbarrier that nothing arrives on, with a short limit. Each CTA
+    then sets the device error word, waits (at the full limit) for its own
+    TMA copies still in flight and returns: pflbm_step and
+    pflbm_ensemble_step must return PFLBM_ERR_DEVICE (8), and the device must
+    stay usable for a normal run in the same process afterwards. Covers the
+    one-node TMA collide (FP32), the node-pair collide (FP16) and the
+    persistent batch collide."""
+    from phasefieldlbm_gb300 import build
+
+    dead = pflbm.load_library(str(build.build_dead_wait()))
+    normal = pflbm.load_library()
+    jet32 = _small_jet(pflbm)
+    jet16 = _small_jet(pflbm)
+    jet16.storage = pflbm.STORAGE_FP16
+    boxes = pflbm.ensemble_configs(3, seed=5)
+    for c in boxes:
+        c.nx = c.ny = c.nz = 32
+        c.radius, c.diam = 6, 12
+    try:
+        pflbm._LIB = dead
+        for cfg, variant in ((jet32, "tma"), (jet16, "tma_pairs")):
+            with pflbm.Simulation(cfg) as s:
+                assert s.collide_variant == variant
+                with pytest.raises(pflbm.PflbmError) as e:
+                    s.step(3)
+                assert e.value.code == 8, e.value
+        with pflbm.Ensemble(boxes) as ens:
+            with pytest.raises(pflbm.PflbmError) as e:
+                ens.step(2)
+            assert e.value.code == 8, e.value
+    finally:
+        pflbm._LIB = normal
+    # the context is intact: a normal run in the same process
+    with pflbm.Simulation(jet32) as s:
+        s.step(5)
+        assert int(s.reduce().nonfinite) == 0

@@ -1,11 +1,18 @@
 """Storage precision against the FP64 oracle at the precision study's error
 grid: the D3Q19 jet, 128x128x512, D = 16, Re = 5000, We = 500, seeded
-uniform inflow noise. After 200 steps:
-  * the library's FP64 path equals the FP64 oracle (rel. L2 <= 1e-10),
-  * FP16 storage (FP32 arithmetic) is within 1e-3 of the FP64 oracle on rho,
-    the centreline u_z and phi, and so is BF16 on rho and phi,
-  * FP32 storage is within 1e-4.
-The oracle runs on the host cores (about two minutes for 200 steps)."""
+uniform inflow noise. After 200 steps (relative L2 of rho, u_z, the
+centreline u_z and phi):
+  * the library's FP64 path equals the FP64 oracle (<= 1e-10),
+  * FP32 storage: rho and phi <= 1e-5; u_z and its centreline within
+    max(1e-5, 2 x floor), the floor being the FP32 oracle's own distance
+    from the FP64 oracle on the same case (about 3e-5 on u_z: the jet's
+    velocity is inflow noise and its growth, which any FP32 evaluation
+    rounds differently),
+  * FP16 storage (FP32 arithmetic) <= 1e-3 on every field,
+  * BF16 storage (8 significant bits): rho and phi <= 1e-3, u_z and its
+    centreline <= BF16_UZ_TOL (the 1e-3 bar is not met by BF16, see the
+    precision study).
+The oracle runs on the host cores (about four minutes for both precisions)."""
 import numpy as np
 import pytest
 
@@ -14,21 +21,34 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 STEPS = 200
+FIELDS = ("rho", "uz", "phi")
+BF16_UZ_TOL = 5e-3
+
+
+def _oracle(pflbm, oracle, fp64):
+    cfg = pflbm.preset("jet_d3q19")
+    o = oracle.OracleSim(cfg, fp64=fp64)
+    o.step(STEPS)
+    out = {f: o.get_field(f) for f in FIELDS}
+    o.close()
+    return out
 
 
 @pytest.fixture(scope="module")
 def oracle_fields(pflbm, oracle):
-    cfg = pflbm.preset("jet_d3q19")
-    o = oracle.OracleSim(cfg, fp64=True)
-    o.step(STEPS)
-    return {f: o.get_field(f) for f in ("rho", "uz", "phi")}
+    return _oracle(pflbm, oracle, True)
+
+
+@pytest.fixture(scope="module")
+def oracle_fp32_floor(pflbm, oracle, oracle_fields):
+    return _errors(_oracle(pflbm, oracle, False), oracle_fields)
 
 
 def _run(pflbm, storage):
     cfg = pflbm.preset("jet_d3q19", storage=storage)
     with pflbm.Simulation(cfg) as s:
         s.step(STEPS)
-        return {f: s.get_field(f, dtype=np.float64) for f in ("rho", "uz", "phi")}
+        return {f: s.get_field(f, dtype=np.float64) for f in FIELDS}
 
 
 def _errors(got, ref):
@@ -44,13 +64,21 @@ def test_fp64_path_is_the_oracle(pflbm, oracle_fields):
     assert max(e.values()) <= 1e-10, e
 
 
-@pytest.mark.parametrize("name,storage,tol,fields", [
-    ("fp32", 0, 1e-4, ("rho", "uz_centreline", "phi", "uz")),
-    ("fp16", 1, 1e-3, ("rho", "uz_centreline", "phi", "uz")),
-    ("bf16", 2, 1e-3, ("rho", "phi")),
+def test_fp32_storage_at_the_fp32_floor(pflbm, oracle_fields, oracle_fp32_floor):
+    e = _errors(_run(pflbm, pflbm.STORAGE_FP32), oracle_fields)
+    floor = oracle_fp32_floor
+    print("fp32", e, "FP32 oracle floor", floor)
+    assert e["rho"] <= 1e-5 and e["phi"] <= 1e-5, e
+    for f in ("uz", "uz_centreline"):
+        assert e[f] <= max(1e-5, 2.0 * floor[f]), (f, e, floor)
+
+
+@pytest.mark.parametrize("name,storage,tols", [
+    ("fp16", 1, {"rho": 1e-3, "uz_centreline": 1e-3, "phi": 1e-3, "uz": 1e-3}),
+    ("bf16", 2, {"rho": 1e-3, "phi": 1e-3, "uz_centreline": BF16_UZ_TOL, "uz": BF16_UZ_TOL}),
 ])
-def test_storage_error_against_fp64_oracle(pflbm, oracle_fields, name, storage, tol, fields):
+def test_storage_error_against_fp64_oracle(pflbm, oracle_fields, name, storage, tols):
     e = _errors(_run(pflbm, storage), oracle_fields)
     print(name, e)
-    for f in fields:
+    for f, tol in tols.items():
         assert e[f] <= tol, (name, f, e)

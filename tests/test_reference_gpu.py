@@ -128,6 +128,36 @@ def test_match_reference_build_at_benchmark_size(pflbm, tmp_path, name, vs):
         assert e[f] <= tol, (f, e, floor)
 
 
+PRESETS = [("jet_d3q27_bench", "jet_d3q27"), ("jet_d3q19_bench", "jet_d3q19")]
+
+
+@pytest.mark.parametrize("name,preset", PRESETS, ids=[p[1] for p in PRESETS])
+def test_match_reference_build_on_bench_preset(pflbm, tmp_path, name, preset):
+    """The benchmark presets themselves (128x128x512, D = 16, Re = 5000,
+    We = 500, gamma = 0.05, seeded uniform +-5% u_z inflow noise) after 100
+    steps: the FP32 library against the reference's own build with the
+    preset's gamma and inflow noise patched in (oracle/ref_build.py). rho,
+    phi <= 1e-5; velocity components within max(1e-5, 2x) the library's own
+    FP32-vs-FP64 difference on the same case."""
+    steps = 100
+    ref = run_reference(name, steps, tmp_path)
+    cfg = pflbm.preset(preset)
+    out = {}
+    for st in (pflbm.STORAGE_FP32, pflbm.STORAGE_FP64):
+        cfg.storage = st
+        with pflbm.Simulation(cfg) as s:
+            s.step(steps)
+            out[st] = {f: s.get_field(f, dtype=np.float64) for f in FIELDS}
+    lib, lib64 = out[pflbm.STORAGE_FP32], out[pflbm.STORAGE_FP64]
+    e = {f: rel_l2(lib[f], ref[f]) for f in FIELDS}
+    floor = {f: rel_l2(lib[f], lib64[f]) for f in FIELDS}
+    e64 = {f: rel_l2(ref[f], lib64[f]) for f in FIELDS}
+    print(preset, "library vs reference build", e, "FP32 floor", floor, "reference build vs FP64 path", e64)
+    for f in FIELDS:
+        tol = max(1e-5, 2.0 * floor[f]) if f in ("ux", "uy", "uz") else 1e-5
+        assert e[f] <= tol, (f, e, floor)
+
+
 def test_fp16_storage_against_reference_fp16_build(pflbm, tmp_path):
     """16-bit storage accuracy at the benchmark jet size: the library's FP16
     path (f - w stored as (f - w)/w, per-direction scaling) and the

@@ -70,6 +70,43 @@ def test_noalloc_reduce_matches_pflbm_reduce(pflbm):
     _compare(got3, want3)
 
 
+@pytest.mark.gpu
+def test_noalloc_reduce_allocates_nothing_and_refuses_host_memory(pflbm):
+    """The property the entry point exists for: after a first call (which
+    loads the library's kernels and the scratch array into the context),
+    further calls leave the device's free memory (cudaMemGetInfo) exactly
+    unchanged. A host buffer passed as a field is refused with
+    PFLBM_ERR_INVALID_ARG before any kernel runs."""
+    torch = pytest.importorskip("torch")
+    lib = pflbm.load_library()
+    cfg = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
+    with pflbm.Simulation(cfg) as s:
+        s.step(10)
+        want, host = s.reduce(), _state(s)
+    nx, ny, nz = int(cfg.nx), int(cfg.ny), int(cfg.nz)
+    dev = {f: torch.from_numpy(np.ascontiguousarray(host[f])).to("cuda") for f in FIELDS}
+    out = torch.zeros(ctypes.sizeof(pflbm.Diag), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    args = [dev[f].data_ptr() for f in FIELDS]
+
+    def call(ptrs):
+        return lib.pflbm_reduce_fields_noalloc(*ptrs, nx, ny, nz, stream, out.data_ptr())
+
+    assert call(args) == 0, lib.pflbm_last_error().decode()  # warm-up
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        assert call(args) == 0, lib.pflbm_last_error().decode()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, (free0, free1)
+    _compare(pflbm.Diag.from_buffer_copy(out.cpu().numpy().tobytes()), want)
+    hbuf = np.ascontiguousarray(host["rho"])
+    rc = call([hbuf.ctypes.data] + args[1:])
+    assert rc == 1, rc  # PFLBM_ERR_INVALID_ARG
+    assert "device memory" in lib.pflbm_last_error().decode()
+
+
 def test_noalloc_reduce_rejects_too_many_planes(pflbm):
     """nz - 2 above PFLBM_NOALLOC_MAX_PLANES (4096) is refused before any CUDA call."""
     lib = pflbm.load_library()
