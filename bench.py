@@ -169,18 +169,25 @@ def cpu_oracle_mlups(cfg, steps: int, warm: int = 1) -> tuple[float, float, int]
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_collide
-# launch from ncu on the 128x128x128 profiling case, scaled to the
-# 128x128x512 workload by the number of interior planes (510 / 126); see
-# profiles/k_collide_tma_jet_d3q27_fp32_128x128x128.md and ..._d3q19_....md.
+# launch, from ncu. jet_d3q27 (the bench workload): measured on the
+# 128x128x512 workload itself, mean of two launches
+# (profiles/k_collide_tma_jet_d3q27_fp32_traffic_128x128x512.md). jet_d3q19:
+# measured on the 128x128x128 profiling case and scaled to 128x128x512 by the
+# interior planes swept (510 / 126;
+# profiles/k_collide_tma_jet_d3q19_fp32_128x128x128.md).
 NCU_COLLIDE_TRAFFIC = {
-    "jet_d3q27": (249.849088e6 + 195.644672e6) * 510 / 126,
+    "jet_d3q27": ((1022.144000e6 + 938.872832e6) + (1021.897472e6 + 935.937536e6)) / 2,
     "jet_d3q19": (179.140864e6 + 127.638528e6) * 510 / 126,
+}
+NCU_TRAFFIC_SOURCE = {
+    "jet_d3q27": "ncu on this 128x128x512 workload (mean of 2 launches)",
+    "jet_d3q19": "ncu on 128x128x128, scaled by interior planes 510/126",
 }
 
 
 def traffic_for(workload: str):
     v = NCU_COLLIDE_TRAFFIC.get(workload)
-    return {"collide_bytes_per_launch": int(v)} if v else None
+    return {"collide_bytes_per_launch": int(v), "source": NCU_TRAFFIC_SOURCE[workload]} if v else None
 
 
 # ---------------------------------------------------------------- arms
@@ -267,11 +274,12 @@ def run_gpu(args, ranks: Ranks) -> dict:
     phase_s = kms[1] / 1e3 / launches
     achieved = ba["collide"] * N / collide_s / 1e9
     step_achieved = ba["total"] * N / ((kms[0] + kms[1]) / 1e3 / launches) / 1e9
-    tr = None if args.nz else traffic_for(args.workload)
+    tr = None if (args.nz or args.storage != "fp32") else traffic_for(args.workload)
     roofline = {
         "bound": "hbm", "kernel": "k_collide", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
         "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
         "traffic": tr.get("collide_bytes_per_launch") if tr else None,
+        "traffic_source": tr.get("source") if tr else None,
         "algorithmic_bytes_per_launch": ba["collide"] * N,
         "avg_launch_ms": round(collide_s * 1e3, 4),
         "peak_source": pk["source"],

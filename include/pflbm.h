@@ -274,10 +274,14 @@ int pflbm_destroy(pflbm_sim *sim);
 
 /* ---- batched ensembles (no counterpart in the reference) ---------------
  * Many independent periodic droplet boxes (FP32, one velocity set, possibly
- * different sizes and physics) advance together: every step is two
- * persistent kernel launches covering all boxes through a device work list,
- * captured in CUDA graphs. Fields and diagnostics are per box and mean the
- * same as for a single simulation. */
+ * different sizes and physics) advance together through a device work list
+ * of (box, column tile, z chunk) items, in CUDA graphs. When every box's rows
+ * are 16-byte aligned (nx a multiple of 4), every step is ONE persistent
+ * cooperative launch: the TMA-fed collide sweep, a bounded grid-wide
+ * barrier, the phase sweep. Otherwise a step is two persistent launches
+ * (plain loads). Fields and diagnostics are per box and mean the same as for
+ * a single simulation. A grid barrier that gives up sets the device error
+ * word: the step returns PFLBM_ERR_DEVICE. */
 typedef struct pflbm_ensemble pflbm_ensemble;
 int pflbm_ensemble_create(const pflbm_config *cfgs, int32_t n_boxes, pflbm_ensemble **out);
 int pflbm_ensemble_init(pflbm_ensemble *ens);
@@ -285,10 +289,20 @@ int pflbm_ensemble_step(pflbm_ensemble *ens, uint64_t nsteps);
 int pflbm_ensemble_step_profiled(pflbm_ensemble *ens, uint64_t nsteps, double *ms);
 int pflbm_ensemble_get_field(pflbm_ensemble *ens, int32_t box, int32_t field_id, void *host_dst, size_t bytes);
 int pflbm_ensemble_reduce(pflbm_ensemble *ens, int32_t box, pflbm_diag *out);
-/* Work granularity: z planes per work item, resident CTAs per SM (1 or 2). */
+/* Work granularity: z planes per work item, resident CTAs per SM (1 up to
+ * what the tile shape lets reside on an SM: 4 for 32x4, 2 for 32x8 and
+ * 64x4, 1 for 32x16; 1 or 2 on the plain-load path). */
 int pflbm_ensemble_set_tuning(pflbm_ensemble *ens, int32_t zchunk, int32_t ctas_per_sm);
-/* Measured autotuner: times each candidate tuning for trial_steps steps,
- * keeps the fastest and re-initialises the ensemble. */
+/* Column tile of the fused TMA step: 32x8 (default), 32x4, 64x4 or 32x16.
+ * The results do not depend on it. PFLBM_ERR_UNSUPPORTED on the plain-load
+ * path (32x8 only) or when the shape does not fit the GPU. */
+int pflbm_ensemble_set_tile(pflbm_ensemble *ens, int32_t tile_x, int32_t tile_y);
+/* The tuning in use (any pointer may be NULL). */
+int pflbm_ensemble_get_tuning(const pflbm_ensemble *ens, int32_t *tile_x, int32_t *tile_y, int32_t *zchunk,
+                              int32_t *ctas_per_sm);
+/* Measured autotuner: times each candidate (tile shape x zchunk x resident
+ * CTAs per SM) for trial_steps steps, keeps the fastest (read it back with
+ * pflbm_ensemble_get_tuning) and re-initialises the ensemble. */
 int pflbm_ensemble_autotune(pflbm_ensemble *ens, int32_t trial_steps, int32_t *best_zchunk, int32_t *best_ctas,
                             double *best_ms);
 int pflbm_ensemble_info(const pflbm_ensemble *ens, uint64_t *total_nodes, int32_t *n_boxes, int32_t *n_items);

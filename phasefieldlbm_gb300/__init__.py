@@ -51,7 +51,7 @@ EXPORTED_SYMBOLS = [
     "pflbm_destroy",
     "pflbm_ensemble_create", "pflbm_ensemble_init", "pflbm_ensemble_step", "pflbm_ensemble_step_profiled",
     "pflbm_ensemble_get_field", "pflbm_ensemble_reduce", "pflbm_ensemble_set_tuning", "pflbm_ensemble_autotune",
-    "pflbm_ensemble_info", "pflbm_ensemble_destroy",
+    "pflbm_ensemble_info", "pflbm_ensemble_destroy", "pflbm_ensemble_set_tile", "pflbm_ensemble_get_tuning",
     "pflbm_reduce_fields_noalloc", "pflbm_write_output_async", "pflbm_set_watchdog",
     "pflbm_closure_create", "pflbm_closure_add_snapshot", "pflbm_closure_num_samples", "pflbm_closure_get_samples",
     "pflbm_closure_set_samples", "pflbm_closure_init_params", "pflbm_closure_get_blob", "pflbm_closure_set_blob",
@@ -185,6 +185,8 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_ensemble_autotune": ([vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double)],
                                     ctypes.c_int),
         "pflbm_ensemble_info": ([vp, ctypes.POINTER(u64), ctypes.POINTER(i32), ctypes.POINTER(i32)], ctypes.c_int),
+        "pflbm_ensemble_set_tile": ([vp, i32, i32], ctypes.c_int),
+        "pflbm_ensemble_get_tuning": ([vp] + [ctypes.POINTER(i32)] * 4, ctypes.c_int),
         "pflbm_ensemble_destroy": ([vp], ctypes.c_int),
         "pflbm_closure_create": ([i32, u64, ctypes.POINTER(vp)], ctypes.c_int),
         "pflbm_closure_add_snapshot": ([vp, vp, i32, ctypes.POINTER(u64)], ctypes.c_int),
@@ -351,11 +353,21 @@ class Ensemble:
     def set_tuning(self, zchunk: int, ctas_per_sm: int):
         _check(self.lib, self.lib.pflbm_ensemble_set_tuning(self._h, zchunk, ctas_per_sm))
 
+    def set_tile(self, tile_x: int, tile_y: int):
+        _check(self.lib, self.lib.pflbm_ensemble_set_tile(self._h, tile_x, tile_y))
+
+    @property
+    def tuning(self) -> dict:
+        v = [ctypes.c_int32() for _ in range(4)]
+        _check(self.lib, self.lib.pflbm_ensemble_get_tuning(self._h, *(ctypes.byref(x) for x in v)))
+        return {"tile": (v[0].value, v[1].value), "zchunk": v[2].value, "ctas_per_sm": v[3].value}
+
     def autotune(self, trial_steps: int = 10) -> dict:
         z, c, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
         _check(self.lib, self.lib.pflbm_ensemble_autotune(self._h, trial_steps, ctypes.byref(z), ctypes.byref(c),
                                                           ctypes.byref(ms)))
-        return {"zchunk": z.value, "ctas_per_sm": c.value, "trial_ms": ms.value}
+        t = self.tuning
+        return {"tile": t["tile"], "zchunk": z.value, "ctas_per_sm": c.value, "trial_ms": ms.value}
 
     @property
     def info(self) -> dict:

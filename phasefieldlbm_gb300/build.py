@@ -140,5 +140,13 @@ def build_dead_wait(jobs: int | None = None) -> Path:
     return build_variant("deadwait", ["-DPFLBM_TEST_DEAD_WAIT"], jobs)
 
 
+def build_dead_grid(jobs: int | None = None) -> Path:
+    """A test build with -DPFLBM_TEST_DEAD_GRID: the grid-wide barrier of the
+    ensemble's fused step polls a flag that nothing sets, with a short limit,
+    so that every CTA gives up, sets the device error word and returns
+    (_build/deadgrid/libpflbm.so)."""
+    return build_variant("deadgrid", ["-DPFLBM_TEST_DEAD_GRID"], jobs)
+
+
 if __name__ == "__main__":
     print(build(verbose=True, force=True))

@@ -54,11 +54,10 @@ Params<T> make_params(const HostParams &h) {
 // boxes (BWN, TY, 1, 1) for the c_x = 0 directions and (BWW, TY, 1, 1) for
 // the others, phi as (x, y, z) with boxes (PBW, PBH, 1). False when the
 // driver entry point is missing or the encoder rejects the layout.
-template <int QQ, class S>
+template <int QQ, class S, class L = TmaLayout<QQ, S>>
 bool encode_collide_maps(const S *f, const typename Store<S>::T *phi, uint64_t nx, uint64_t ny, uint64_t nz,
                          CUtensorMap &fmapn, CUtensorMap &fmapw, CUtensorMap &phimap) {
     using T = typename Store<S>::T;
-    using L = TmaLayout<QQ, S>;
     using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -78,8 +77,10 @@ bool encode_collide_maps(const S *f, const typename Store<S>::T *phi, uint64_t n
     const uint64_t N = nx * ny * nz;
     const cuuint64_t fdim[4] = {nx, ny, nz, cuuint64_t(QQ)};
     const cuuint64_t fstr[3] = {nx * sizeof(S), nx * ny * sizeof(S), N * sizeof(S)};
-    const cuuint32_t fboxn[4] = {cuuint32_t(L::BWN), cuuint32_t(TY), 1, 1};
-    const cuuint32_t fboxw[4] = {cuuint32_t(L::BWW), cuuint32_t(TY), 1, 1};
+    // boxes of the layout's tile: the TMA writes exactly what L's shared-memory
+    // plan and transaction count expect
+    const cuuint32_t fboxn[4] = {cuuint32_t(L::BWN), cuuint32_t(L::TY), 1, 1};
+    const cuuint32_t fboxw[4] = {cuuint32_t(L::BWW), cuuint32_t(L::TY), 1, 1};
     const cuuint32_t one4[4] = {1, 1, 1, 1};
     for (int k = 0; k < 2; ++k)
         if (enc(k ? &fmapw : &fmapn, ft, 4, const_cast<S *>(f), fdim, fstr, k ? fboxw : fboxn, one4,

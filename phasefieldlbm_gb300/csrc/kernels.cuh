@@ -47,6 +47,7 @@
 #include "closure_net.cuh"
 #include "lattice.cuh"
 #include "params.cuh"
+#include "sround.cuh"
 #include "stencil.cuh"
 #include "tile.h"
 
@@ -168,18 +169,29 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
             return o;
         };
         // collision + streaming (src/lbm.cu:172-207); direction q's array
-        // starts at f_dst + q N
-        if (PFLBM_GUARD(base < N, b.err))
-            Store<S>::store(b.f_dst, node, collide_rest<QQ, T>(k), static_cast<T>(1.0 / weight<QQ>(0)));
+        // starts at f_dst + q N. BF16 storage rounds stochastically
+        // (sround.cuh), with the bits of this node's half of its pair.
+        constexpr bool kSR = std::is_same<S, __nv_bfloat16>::value;
+        uint32_t sr_seed = 0u;
+        if constexpr (kSR) sr_seed = sr_pair_seed(node >> 1, t);
+        const uint32_t sr_shift = (node & 1u) ? 16u : 0u;
+        auto put = [&](int q, uint32_t idx, T v) {
+            const T inv_w = static_cast<T>(1.0 / weight<QQ>(q));
+            if constexpr (kSR) {
+                const uint32_t r = (sr_dir_bits(sr_seed, q) >> sr_shift) & 0xFFFFu;
+                reinterpret_cast<uint16_t *>(b.f_dst + uint64_t(q) * N)[idx] = bf16_bits_sr(v * inv_w, r);
+            } else {
+                Store<S>::store(b.f_dst + uint64_t(q) * N, idx, v, inv_w);
+            }
+        };
+        if (PFLBM_GUARD(base < N, b.err)) put(0, node, collide_rest<QQ, T>(k));
 #pragma unroll
         for (int q = 1; q < QQ; q += 2) {
             T a, c;
             collide_pair<QQ, T>(q, k, a, c);
             const uint32_t iq = dst_node(q), iqb = dst_node(q + 1);
-            if (PFLBM_GUARD(iq < N, b.err))
-                Store<S>::store(b.f_dst + uint64_t(q) * N, iq, a, static_cast<T>(1.0 / weight<QQ>(q)));
-            if (PFLBM_GUARD(iqb < N, b.err))
-                Store<S>::store(b.f_dst + uint64_t(q + 1) * N, iqb, c, static_cast<T>(1.0 / weight<QQ>(q + 1)));
+            if (PFLBM_GUARD(iq < N, b.err)) put(q, iq, a);
+            if (PFLBM_GUARD(iqb < N, b.err)) put(q + 1, iqb, c);
         }
         // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J)
         const T sharp = p.gamma * phi * (T(1) - phi);

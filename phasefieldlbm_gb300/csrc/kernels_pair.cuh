@@ -13,8 +13,8 @@
 // Interior node pairs store each direction as one 8-byte (FP32) or 4-byte
 // (16-bit) word. The two pairs at the periodic x edges, where one node of the
 // pair is a ghost, store the active node alone with its wrap offsets. With
-// 16-bit storage the three reciprocals of a node use the approximate hardware
-// reciprocal. (Evaluating the collision directly in the stored unknown f'/w_q
+// 16-bit storage the three reciprocals of a node and the square root of the
+// phi-gradient norm use the approximate hardware operations. (Evaluating the collision directly in the stored unknown f'/w_q
 // saves the rescaling multiply but was measurably less accurate against the
 // FP64 path: rho 2.6x, u_z 1.4x the error of the one-node kernel after 400
 // jet steps. The exact scaled values round to 16 bits coherently, where the
@@ -299,8 +299,9 @@ __device__ __forceinline__ V2 collide_rest2(const Ctx2<QQ> &k) {
 // is formed.
 template <int QQ, bool JET, class S>
 __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const StepBuffers<S, float> &b, int xa,
-                                                  int y, int z, bool act_a, bool act_b, const V2 (&pop)[QQ], V2 phi,
-                                                  V2 n_x, V2 n_y, V2 n_z, V2 ind, V2 curvature) {
+                                                  int y, int z, uint32_t t, bool act_a, bool act_b,
+                                                  const V2 (&pop)[QQ], V2 phi, V2 n_x, V2 n_y, V2 n_z, V2 ind,
+                                                  V2 curvature) {
     constexpr bool FAST = PairStore<S>::kScaled;  // 16-bit storage: approximate reciprocals
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const uint64_t N = p.N;
@@ -400,6 +401,11 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
         ez_p = (z == nz - 2) ? 0u - uint32_t(nz - 2) * plane : 0u;
         ez_m = (z == 1) ? uint32_t(nz - 2) * plane : 0u;
     }
+    // BF16 storage rounds stochastically (sround.cuh): 16 random bits per
+    // node and direction, the same bits the one-node kernel draws
+    constexpr bool kSR = std::is_same<S, __nv_bfloat16>::value;
+    uint32_t sr_seed = 0u;
+    if constexpr (kSR) sr_seed = sr_pair_seed(node_a >> 1, t);
     if (both) {
         // interior pair: the x offsets vanish for both nodes
         auto put = [&](int q, V2 v) {
@@ -408,8 +414,15 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
             if (kCY[q] < 0) d += ey_m;
             if (kCZ[q] > 0) d += ez_p;
             if (kCZ[q] < 0) d += ez_m;
-            if (PFLBM_GUARD(d + 1 < N, b.err))
-                PairStore<S>::store2(b.f_dst + uint64_t(q) * N + d, v, static_cast<float>(1.0 / weight<QQ>(q)));
+            if (!PFLBM_GUARD(d + 1 < N, b.err)) return;
+            const float inv_w = static_cast<float>(1.0 / weight<QQ>(q));
+            if constexpr (kSR) {
+                const V2 sc = v * V2(inv_w);
+                *reinterpret_cast<uint32_t *>(b.f_dst + uint64_t(q) * N + d) =
+                    bf16x2_bits_sr(sc.v.x, sc.v.y, sr_dir_bits(sr_seed, q));
+            } else {
+                PairStore<S>::store2(b.f_dst + uint64_t(q) * N + d, v, inv_w);
+            }
         };
         put(0, collide_rest2<QQ>(k));
 #pragma unroll
@@ -433,9 +446,15 @@ __device__ __forceinline__ void collide_node_pair(const Params<float> &p, const 
             if (kCY[q] < 0) d += ey_m;
             if (kCZ[q] > 0) d += ez_p;
             if (kCZ[q] < 0) d += ez_m;
-            if (PFLBM_GUARD(d < N, b.err))
-                PairStore<S>::store1(b.f_dst + uint64_t(q) * N + d, lb ? v.v.y : v.v.x,
-                                     static_cast<float>(1.0 / weight<QQ>(q)));
+            if (!PFLBM_GUARD(d < N, b.err)) return;
+            const float inv_w = static_cast<float>(1.0 / weight<QQ>(q));
+            const float vv = lb ? v.v.y : v.v.x;
+            if constexpr (kSR) {
+                const uint32_t r = sr_dir_bits(sr_seed, q);
+                reinterpret_cast<uint16_t *>(b.f_dst + uint64_t(q) * N)[d] = bf16_bits_sr(vv * inv_w, lb ? (r >> 16) : (r & 0xFFFFu));
+            } else {
+                PairStore<S>::store1(b.f_dst + uint64_t(q) * N + d, vv, inv_w);
+            }
         };
         put(0, collide_rest2<QQ>(k));
 #pragma unroll
@@ -474,6 +493,7 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
     const bool rowok = y >= 1 && y <= ny - 2;
     const bool act_a = rowok && xa >= 1 && xa <= nx - 2;
     const bool act_b = rowok && xa + 1 >= 1 && xa + 1 <= nx - 2;
+    const uint32_t t = b.step_in ? static_cast<uint32_t>(*b.step_in) : b.t_fixed;
 
     auto pslot = [&](int zp) { return (zp + 2 * R) % R; };
     auto phi_at = [&](int slot, int ly, int lx) -> T & {
@@ -585,7 +605,7 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
             // populations as f' = f - w: FP32 stores f', 16-bit storage f'/w
             pop[q] = PairStore<S>::kScaled ? raw * V2(static_cast<float>(weight<QQ>(q))) : raw;
         }
-        collide_node_pair<QQ, JET, S>(p, b, xa, y, z, act_a, act_b, pop, phi, n_x, n_y, n_z, ind, curvature);
+        collide_node_pair<QQ, JET, S>(p, b, xa, y, z, t, act_a, act_b, pop, phi, n_x, n_y, n_z, ind, curvature);
     }
     seq += uint32_t(ze - zb);
     return true;

@@ -32,6 +32,19 @@ constexpr uint32_t kWaitLimit = 1u << 22;
 constexpr int NXP = NX_ / 2;  // x-adjacent entry pairs per row of the normal ring
 static_assert(NX_ % 2 == 0, "normal ring pairs");
 
+// Column tile of the TMA collide: TXv x TYv nodes, one thread per node
+// (blockDim = (TXv, TYv)). The single-box kernels use the build's tile
+// (PFLBM_TILE_X x PFLBM_TILE_Y); the batched ensemble instantiates several
+// and lets its autotuner choose.
+template <int TXv, int TYv>
+struct TileShape {
+    static constexpr int TX = TXv, TY = TYv, NT = TXv * TYv;
+    static constexpr int NX = TXv + 2, NY = TYv + 2;  // normal ring: tile + halo 1
+    static constexpr int NXP = NX / 2;                 // x-adjacent entry pairs per ring row
+    static_assert(TXv % 32 == 0 && NT <= 1024 && NX % 2 == 0, "tile shape");
+};
+using DefaultTile = TileShape<TX, TY>;
+
 // n^ and |grad phi| of the normal-ring entries (lx, ly) and (lx + 1, ly), lx
 // even, with packed FP32x2 arithmetic: `e(dx, dy, dz)` points at the phi
 // element of the first entry's neighbour (dx, dy, dz). The +-1 x neighbours
@@ -67,9 +80,12 @@ __host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~si
 // halo is read), TX + XU wide otherwise, where XU is the 16-byte alignment
 // unit of the x coordinate, starting at x0 - XU for c_x = +1 (halo column
 // x0 - 1) and at x0 for c_x = -1 (halo column x0 + TX).
-template <int QQ, class S, int NS>
+template <int QQ, class S, int NS, class RT = typename Store<S>::T, class G = DefaultTile>
 struct TmaPlan {
     using T = typename Store<S>::T;
+    using RingT = RT;  // element type of the normal and |grad phi| rings
+    using Tile = G;
+    static constexpr int TX = G::TX, TY = G::TY, NX_ = G::NX, NY_ = G::NY;
     static constexpr int kStages = NS;
     static constexpr int XU = 16 / int(sizeof(S));  // elements per 16 bytes
     static constexpr int BWN = TX;                  // box width, c_x = 0
@@ -101,10 +117,10 @@ struct TmaPlan {
     static constexpr size_t off_phi = align128(NS * stage_bytes);
     // n^ (3 components) of 4 planes on the tile + halo 1
     static constexpr size_t off_n = align128(off_phi + kPhiSlots * phi_slot_bytes);
-    static constexpr size_t n_bytes = size_t(3) * 4 * NY_ * NX_ * sizeof(T);
+    static constexpr size_t n_bytes = size_t(3) * 4 * NY_ * NX_ * sizeof(RT);
     // |grad phi| of 3 planes, tile rows only (rows of the halo width)
     static constexpr size_t off_ind = align128(off_n + n_bytes);
-    static constexpr size_t ind_bytes = size_t(3) * TY * NX_ * sizeof(T);
+    static constexpr size_t ind_bytes = size_t(3) * TY * NX_ * sizeof(RT);
     static constexpr size_t off_bar = align128(off_ind + ind_bytes);
     // NS mbarriers, the abort flag, and at off_bar + 64 the test build's
     // never-arriving barrier (plane_wait)
@@ -140,18 +156,19 @@ struct CollideOccupancy {
         sizeof(typename Store<S>::T) == 8 ? 1 : (sizeof(S) == 2 && QQ == 19 ? 3 : PFLBM_COLLIDE_MIN_BLOCKS);
 };
 
-template <int QQ, class S>
+template <int QQ, class S, class G = DefaultTile>
 struct TmaStages {
     static constexpr size_t kBudget = sizeof(typename Store<S>::T) == 8 ? 227u * 1024u
                                       : CollideOccupancy<QQ, S>::value == 3 ? 74u * 1024u
                                                                             : size_t(PFLBM_TMA_SMEM_BUDGET);
-    static constexpr int value = TmaPlan<QQ, S, 4>::total <= kBudget   ? 4
-                                 : TmaPlan<QQ, S, 3>::total <= kBudget ? 3
-                                                                       : 2;
+    using RT = typename Store<S>::T;
+    static constexpr int value = TmaPlan<QQ, S, 4, RT, G>::total <= kBudget   ? 4
+                                 : TmaPlan<QQ, S, 3, RT, G>::total <= kBudget ? 3
+                                                                              : 2;
 };
 
-template <int QQ, class S>
-using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S>::value>;
+template <int QQ, class S, class G = DefaultTile>
+using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S, G>::value, typename Store<S>::T, G>;
 
 // Barriers of the TMA pipeline: once per CTA, before its first tile.
 template <int QQ, class S, class L = TmaLayout<QQ, S>>
@@ -190,14 +207,15 @@ __device__ __forceinline__ bool plane_wait(unsigned char *smem, uint64_t *bar, u
 // parity = (seq / NS) & 1), so that a persistent CTA can run tile after tile
 // on the same barriers; every stage issued for a tile is consumed by it.
 // Returns false when a bounded wait gave up (error word set, copies drained).
-template <int QQ, bool JET, class S, int MODE>
+template <int QQ, bool JET, class S, int MODE, class G = DefaultTile, class L = TmaLayout<QQ, S, G>>
 __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>::T> &p,
                                                  const StepBuffers<S, typename Store<S>::T> &b,
                                                  const CUtensorMap *fmapn_p, const CUtensorMap *fmapw_p,
                                                  const CUtensorMap *phimap_p, int x0, int y0, int zb, int ze,
                                                  unsigned char *smem, uint32_t &seq, float *s_mlp = nullptr) {
     using T = typename Store<S>::T;
-    using L = TmaLayout<QQ, S>;
+    static_assert(std::is_same<typename L::Tile, G>::value, "plan for this tile");
+    constexpr int TX = G::TX, TY = G::TY, NT = G::NT, NX_ = G::NX, NY_ = G::NY, NXP = G::NXP;
     S *s_f = reinterpret_cast<S *>(smem + L::off_f);
     T *s_phi = reinterpret_cast<T *>(smem + L::off_phi);
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);

@@ -45,6 +45,12 @@ __device__ __forceinline__ V2 op_mul(V2 a, V2 b) { return a * b; }
 __device__ __forceinline__ V2 op_add(V2 a, V2 b) { return a + b; }
 __device__ __forceinline__ V2 op_fma(V2 a, V2 b, V2 c) { return fma2(a, b, c); }
 __device__ __forceinline__ V2 op_sqrt(V2 a) { return V2(sqrtf(a.v.x), sqrtf(a.v.y)); }
+__device__ __forceinline__ V2 op_sqrt_approx(V2 a) {
+    float rx, ry;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(rx) : "f"(a.v.x));
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(ry) : "f"(a.v.y));
+    return V2(rx, ry);
+}
 template <bool FAST>
 __device__ __forceinline__ V2 op_recip(V2 a) { return recip2<FAST>(a); }
 

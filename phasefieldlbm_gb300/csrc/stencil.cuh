@@ -22,6 +22,15 @@ __device__ __forceinline__ double op_add(double a, double b) { return __dadd_rn(
 __device__ __forceinline__ float op_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double op_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float op_sqrt(float a) { return sqrtf(a); }
+// approximate square root (PTX sqrt.approx.f32, about 2 ulp): the FAST
+// stencils of 16-bit storage runs, whose stored values carry 11 or 8
+// significant bits
+__device__ __forceinline__ float op_sqrt_approx(float a) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+__device__ __forceinline__ double op_sqrt_approx(double a) { return sqrt(a); }
 __device__ __forceinline__ double op_sqrt(double a) { return sqrt(a); }
 template <bool FAST>
 __device__ __forceinline__ float op_recip(float a) {
@@ -82,12 +91,16 @@ __device__ __forceinline__ T lattice_grad(const Get &v) {
 
 // Interface normal n = grad phi / (|grad phi| + 1e-9) and |grad phi| from
 // the lattice gradient sums (src/phaseField.cuh:67-118), in one fixed
-// rounding order for the scalar and packed evaluations.
+// rounding order for the scalar and packed evaluations. FAST (16-bit
+// storage runs): approximate square root and reciprocal.
 template <bool FAST, class T>
 __device__ __forceinline__ void unit_normal(T sx, T sy, T sz, T &nx, T &ny, T &nz, T &ind) {
     const T gx = op_mul(static_cast<T>(3.0), sx), gy = op_mul(static_cast<T>(3.0), sy),
             gz = op_mul(static_cast<T>(3.0), sz);
-    ind = op_sqrt(op_fma(gx, gx, op_fma(gy, gy, op_mul(gz, gz))));
+    if constexpr (FAST)
+        ind = op_sqrt_approx(op_fma(gx, gx, op_fma(gy, gy, op_mul(gz, gz))));
+    else
+        ind = op_sqrt(op_fma(gx, gx, op_fma(gy, gy, op_mul(gz, gz))));
     const T inv = op_recip<FAST>(op_add(ind, static_cast<T>(1e-9)));
     nx = op_mul(gx, inv);
     ny = op_mul(gy, inv);

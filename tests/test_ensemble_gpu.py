@@ -55,7 +55,9 @@ def test_autotune_and_mass(pflbm):
     cfgs = small_batch(pflbm, n=6)
     with pflbm.Ensemble(cfgs) as ens:
         best = ens.autotune(trial_steps=4)
-        assert best["zchunk"] in (4, 8, 16, 32, 64) and best["ctas_per_sm"] in (1, 2)
+        assert best["zchunk"] in (4, 8, 16, 32, 64) and best["ctas_per_sm"] in (1, 2, 3, 4)
+        assert best["tile"] in ((32, 8), (32, 4), (64, 4), (32, 16))
+        assert ens.tuning == {"tile": best["tile"], "zchunk": best["zchunk"], "ctas_per_sm": best["ctas_per_sm"]}
         ens.step(1)
         m0 = [ens.reduce(k).phi_mass for k in range(len(cfgs))]
         ens.step(100)
@@ -104,3 +106,23 @@ def test_unaligned_boxes_use_the_plain_path(pflbm):
             for f in FIELDS:
                 tol = 1e-6 if f in ("rho", "phi") else 1e-3
                 assert rel_l2(got[k][f], s.get_field(f)) <= tol, (k, f)
+
+
+@pytest.mark.parametrize("vs", [19, 27])
+def test_tile_shapes_bit_identical(pflbm, vs):
+    """The fused step's tile shapes (32x8, 32x4, 64x4, 32x16) change only how
+    the grid is cut into work items: every node evaluates the same stencils
+    and collision, so the fields are bit-identical whatever the shape."""
+    cfgs = small_batch(pflbm, n=4, vs=vs)
+    out = {}
+    for tile in ((32, 8), (32, 4), (64, 4), (32, 16)):
+        with pflbm.Ensemble(cfgs) as ens:
+            ens.set_tile(*tile)
+            assert ens.tuning["tile"] == tile
+            ens.step(19)
+            out[tile] = [ens.get_field(k, "phi") for k in range(len(cfgs))] + [
+                ens.get_field(k, "uz") for k in range(len(cfgs))]
+    ref = out[(32, 8)]
+    for tile, v in out.items():
+        for a, b in zip(v, ref):
+            assert np.array_equal(a, b), tile

@@ -102,3 +102,30 @@ def test_bounded_tma_wait_runs_out_and_reports(pflbm):
     with pflbm.Simulation(jet32) as s:
         s.step(5)
         assert int(s.reduce().nonfinite) == 0
+
+
+def test_ensemble_grid_barrier_runs_out_and_reports(pflbm):
+    """The grid-wide barrier of the ensemble's fused step, made to run out:
+    the test build _build/deadgrid (-DPFLBM_TEST_DEAD_GRID) polls a flag that
+    nothing sets, with a short limit. Every CTA sets the device error word
+    and returns; pflbm_ensemble_step returns PFLBM_ERR_DEVICE (8) and a
+    normal ensemble in the same process runs afterwards."""
+    from phasefieldlbm_gb300 import build
+
+    dead = pflbm.load_library(str(build.build_dead_grid()))
+    normal = pflbm.load_library()
+    boxes = pflbm.ensemble_configs(3, seed=5)
+    for c in boxes:
+        c.nx = c.ny = c.nz = 32
+        c.radius, c.diam = 6, 12
+    try:
+        pflbm._LIB = dead
+        with pflbm.Ensemble(boxes) as ens:
+            with pytest.raises(pflbm.PflbmError) as e:
+                ens.step(2)
+            assert e.value.code == 8, e.value
+    finally:
+        pflbm._LIB = normal
+    with pflbm.Ensemble(boxes) as ens:
+        ens.step(3)
+        assert all(int(ens.reduce(k).nonfinite) == 0 for k in range(len(boxes)))

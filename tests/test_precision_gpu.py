@@ -9,9 +9,12 @@ centreline u_z and phi):
     velocity is inflow noise and its growth, which any FP32 evaluation
     rounds differently),
   * FP16 storage (FP32 arithmetic) <= 1e-3 on every field,
-  * BF16 storage (8 significant bits): rho and phi <= 1e-3, u_z and its
-    centreline <= BF16_UZ_TOL (the 1e-3 bar is not met by BF16, see the
-    precision study).
+  * BF16 storage (8 significant bits, stochastic rounding): rho and phi
+    <= 1e-3, u_z and its centreline <= BF16_UZ_TOL = 4e-3. The 1e-3 bar is
+    not met by BF16: measured 2.9e-3 (u_z) and 1.7e-3 (centreline) here;
+    round-to-nearest gives 2.1e-3 / 1.7e-3 at 200 steps but grows linearly
+    (2.7e-2 / 3.1e-2 at 2000 steps, against 9.9e-3 / 4.1e-3 with stochastic
+    rounding).
 The oracle runs on the host cores (about four minutes for both precisions)."""
 import numpy as np
 import pytest
@@ -22,7 +25,7 @@ pytestmark = pytest.mark.gpu
 
 STEPS = 200
 FIELDS = ("rho", "uz", "phi")
-BF16_UZ_TOL = 5e-3
+BF16_UZ_TOL = 4e-3
 
 
 def _oracle(pflbm, oracle, fp64):
