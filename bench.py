@@ -356,6 +356,11 @@ def run_gpu(args, ranks: Ranks) -> dict:
                                   "collide_ms": round(k2[0] / (2 * inner), 4), "phase_ms": round(k2[1] / (2 * inner), 4),
                                   "steps": vsteps, "rel_l2_vs_fp64": errors(wl, s2)}
 
+        # the batched droplet ensemble (64 seeded boxes, 2000 steps, autotuned,
+        # one cooperative launch per step) against the same boxes run one
+        # after another as single simulations
+        variants["ensemble64_d3q19_fp32"] = run_ensemble_study(args, device=cfg.device)
+
     cpu = None
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu_baseline:
         # a bounded sample of about 10 s of host work: as many full-grid steps
@@ -553,31 +558,45 @@ def run_closure_study(args) -> dict:
     return out
 
 
-def run_ensemble_study(args) -> dict:
+def run_ensemble_study(args, device: int = 0) -> dict:
     """The batched droplet ensemble: 64 seeded periodic boxes (edges in
-    {32,48,64,80,96}), autotuned, `steps` steps in the persistent
-    graph-captured launches, against the same boxes run one after another as
-    single simulations (each with its own captured graph)."""
+    {32,48,64,80,96}), autotuned (tile shape, z chunk, resident CTAs), `steps`
+    steps of one persistent cooperative launch each, graph-captured, against
+    the same boxes run one after another as single simulations (each with
+    its own captured graph)."""
     import phasefieldlbm_gb300 as pf
 
     steps = args.ensemble_steps
     cfgs = pf.ensemble_configs(64)
+    for c in cfgs:
+        c.device = device
     total_nodes = sum(c.nodes for c in cfgs)
     with pf.Ensemble(cfgs) as ens:
-        tune = ens.autotune(10)
+        if getattr(args, "ensemble_tuning", ""):
+            # a fixed tuning "TXxTY,zchunk,ctas" instead of the autotuner
+            t, zc, ctas = args.ensemble_tuning.split(",")
+            ens.set_tile(*(int(v) for v in t.split("x")))
+            ens.set_tuning(int(zc), int(ctas))
+            tune = {**ens.tuning, "trial_ms": None}
+        else:
+            tune = ens.autotune(10)
         ens.step(10)
         ms = ens.step_profiled(steps)
         diverged = [b for b in range(len(cfgs)) if int(ens.reduce(b).nonfinite) > 0]
-    seq_ms = 0.0
-    for c in cfgs:
-        with pf.Simulation(c) as s:
-            s.step(10)
-            tot, _ = s.step_profiled(steps)
-            seq_ms += tot
+    seq_ms = None
+    if not getattr(args, "ensemble_no_sequential", False):
+        seq_ms = 0.0
+        for c in cfgs:
+            with pf.Simulation(c) as s:
+                s.step(10)
+                tot, _ = s.step_profiled(steps)
+                seq_ms += tot
+    tune["tile"] = list(tune["tile"])
     return {"study": "ensemble", "boxes": len(cfgs), "nodes": total_nodes, "steps": steps, "autotune": tune,
             "batched_mlups": round(total_nodes * steps / (ms / 1e3) / 1e6, 1),
-            "sequential_mlups": round(total_nodes * steps / (seq_ms / 1e3) / 1e6, 1),
-            "speedup": round(seq_ms / ms, 3), "diverged_boxes": diverged}
+            "sequential_mlups": round(total_nodes * steps / (seq_ms / 1e3) / 1e6, 1) if seq_ms else None,
+            "speedup": round(seq_ms / ms, 3) if seq_ms else None, "diverged_boxes": diverged,
+            "launches_per_step": 1}
 
 
 def main():
@@ -595,6 +614,9 @@ def main():
                     help="population storage of the workload")
     ap.add_argument("--study", choices=["precision", "closure", "ensemble"], help="run a study instead of the bench line")
     ap.add_argument("--ensemble-steps", type=int, default=2000)
+    ap.add_argument("--ensemble-tuning", default="", help="ensemble study: fixed tuning TXxTY,zchunk,ctas (no autotune)")
+    ap.add_argument("--ensemble-no-sequential", action="store_true",
+                    help="ensemble study: skip the sequential single-box comparison (profiling captures)")
     ap.add_argument("--fine-grid", default="256,256,1024,32", help="closure study: fine nx,ny,nz,D")
     ap.add_argument("--snapshots", type=int, default=20)
     ap.add_argument("--snapshot-every", type=int, default=500)

@@ -318,7 +318,9 @@ __device__ __forceinline__ void collide_tile(const Params<typename Store<S>::T> 
                 auto v = [&](int dx, int dy, int dz) -> T {
                     return s_phi[dz < 0 ? sm : (dz > 0 ? sp : s0)][ly + 1 + dy][lx + 1 + dx];
                 };
-                unit_normal<false>(lattice_grad<QQ, 0, T>(v), lattice_grad<QQ, 1, T>(v), lattice_grad<QQ, 2, T>(v), nxv,
+                // FP32: approximate square root and reciprocal, as the TMA
+                // kernel's packed normals (bit-identical); FP64: IEEE
+                unit_normal<sizeof(T) == 4>(lattice_grad<QQ, 0, T>(v), lattice_grad<QQ, 1, T>(v), lattice_grad<QQ, 2, T>(v), nxv,
                                    nyv, nzv, ind);
             }
             s_n[0][sn][ly][lx] = nxv;

@@ -13,8 +13,9 @@
 // Interior node pairs store each direction as one 8-byte (FP32) or 4-byte
 // (16-bit) word. The two pairs at the periodic x edges, where one node of the
 // pair is a ghost, store the active node alone with its wrap offsets. With
-// 16-bit storage the three reciprocals of a node and the square root of the
-// phi-gradient norm use the approximate hardware operations. (Evaluating the collision directly in the stored unknown f'/w_q
+// 16-bit storage the three reciprocals of a node use the approximate hardware
+// reciprocal; in every run the phi normals use the approximate square root
+// and reciprocal, as the one-node kernels do. (Evaluating the collision directly in the stored unknown f'/w_q
 // saves the rescaling multiply but was measurably less accurate against the
 // FP64 path: rho 2.6x, u_z 1.4x the error of the one-node kernel after 400
 // jet steps. The exact scaled values round to 16 bits coherently, where the
@@ -544,7 +545,7 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
             const bool va = yok && gxa >= 1 && gxa <= nx - 2;
             const bool vb = yok && gxa + 1 >= 1 && gxa + 1 <= nx - 2;
             V2 nxv, nyv, nzv, indv;
-            normal_pair<QQ, PairStore<S>::kScaled>(
+            normal_pair<QQ, true>(
                 [&](int dx, int dy, int dz) -> const T * {
                     return &phi_at(dz < 0 ? sm : (dz > 0 ? sp : sn), ly + 1 + dy, lx + L::PXO - 1 + dx);
                 },

@@ -283,7 +283,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
                 const int gxa = x0 - 1 + lx, gy = y0 - 1 + ly;
                 const bool yok = zok && gy >= 1 && gy <= ny - 2;
                 V2 nxv, nyv, nzv, ind;
-                normal_pair<QQ, false>(
+                normal_pair<QQ, true>(
                     [&](int dx, int dy, int dz) -> const float * {
                         return &phi_at(dz < 0 ? sm : (dz > 0 ? sp : sn), ly + 1 + dy, lx + L::PXO - 1 + dx);
                     },

@@ -24,10 +24,10 @@ __device__ __forceinline__ uint32_t sr_pair_seed(uint32_t pair, uint32_t t) {
     return hash32(pair * 0x9E3779B1u ^ t * 0x85EBCA77u ^ 0xC2B2AE3Du);
 }
 
-// 32 random bits for direction q of the pair: the low 16 bits for the even
-// node, the high 16 bits for the odd one.
-__device__ __forceinline__ uint32_t sr_dir_bits(uint32_t seed, int q) {
-    uint32_t x = seed + uint32_t(q) * 0x9E3779B9u;
+// A fixed, well-mixed 32-bit constant per direction (a compile-time
+// immediate for a compile-time q).
+__host__ __device__ constexpr uint32_t sr_dir_const(int q) {
+    uint32_t x = uint32_t(q + 1) * 0x9E3779B9u;
     x ^= x >> 16;
     x *= 0x7FEB352Du;
     x ^= x >> 15;
@@ -35,6 +35,12 @@ __device__ __forceinline__ uint32_t sr_dir_bits(uint32_t seed, int q) {
     x ^= x >> 16;
     return x;
 }
+
+// 32 random bits for direction q of the pair: the low 16 bits for the even
+// node, the high 16 bits for the odd one. The directions of a pair share the
+// pair's hash, each XORed with its own constant: every direction's bits are
+// uniform (an unbiased rounding) at one instruction per direction.
+__device__ __forceinline__ uint32_t sr_dir_bits(uint32_t seed, int q) { return seed ^ sr_dir_const(q); }
 
 // v rounded to BF16 with 16 random bits r: the discarded low half of v's
 // bits plus r carries into the kept half with probability (low half) / 2^16.

@@ -23,8 +23,7 @@ __device__ __forceinline__ float op_fma(float a, float b, float c) { return __fm
 __device__ __forceinline__ double op_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float op_sqrt(float a) { return sqrtf(a); }
 // approximate square root (PTX sqrt.approx.f32, about 2 ulp): the FAST
-// stencils of 16-bit storage runs, whose stored values carry 11 or 8
-// significant bits
+// normals of FP32-arithmetic runs
 __device__ __forceinline__ float op_sqrt_approx(float a) {
     float r;
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
@@ -91,8 +90,10 @@ __device__ __forceinline__ T lattice_grad(const Get &v) {
 
 // Interface normal n = grad phi / (|grad phi| + 1e-9) and |grad phi| from
 // the lattice gradient sums (src/phaseField.cuh:67-118), in one fixed
-// rounding order for the scalar and packed evaluations. FAST (16-bit
-// storage runs): approximate square root and reciprocal.
+// rounding order for the scalar and packed evaluations. FAST (every FP32
+// arithmetic run): approximate square root and reciprocal (PTX sqrt.approx,
+// __fdividef; about 2 ulp, far below the FP32 rounding floor of the fields
+// the normals feed); FP64 runs keep the IEEE operations.
 template <bool FAST, class T>
 __device__ __forceinline__ void unit_normal(T sx, T sy, T sz, T &nx, T &ny, T &nz, T &ind) {
     const T gx = op_mul(static_cast<T>(3.0), sx), gy = op_mul(static_cast<T>(3.0), sy),

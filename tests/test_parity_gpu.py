@@ -237,6 +237,11 @@ PAIR_TOL = {  # rel. L2 of the node-pair kernel against the one-node kernel: rho
     1: (1e-5, 5e-5, 2e-3),    # FP16: the last stored bit differs now and then
     2: (5e-5, 5e-4, 1e-2),    # BF16
 }
+# FP32 droplets: the velocity is spurious currents, whose FP32 rounding floor
+# (the oracle's own FP32-vs-FP64 difference) reaches 5e-5; the reordered
+# algebra's rounding shows as u 2.8e-5 and phi 2.2e-6 after 60 steps of the
+# R = 10 droplet
+PAIR_TOL_FP32_DROPLET = (1e-6, 5e-6, 6e-5)
 
 
 @pytest.mark.parametrize("case,vs,storage", [
@@ -270,7 +275,7 @@ def test_pair_kernel_matches_one_node_kernel(pflbm, monkeypatch, case, vs, stora
             assert s.collide_variant == ("tma_pairs" if mode == "pair" else "tma")
             s.step(steps)
             out[mode] = {f: s.get_field(f, dtype=np.float64) for f in BASIC}
-    t_rho, t_phi, t_u = PAIR_TOL[storage]
+    t_rho, t_phi, t_u = PAIR_TOL_FP32_DROPLET if (storage == 0 and case == "droplet") else PAIR_TOL[storage]
     e = {f: rel_l2(out["pair"][f], out["one"][f]) for f in BASIC}
     e["u"] = rel_l2(np.stack([out["pair"][f] for f in ("ux", "uy", "uz")]),
                     np.stack([out["one"][f] for f in ("ux", "uy", "uz")]))
