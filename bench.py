@@ -527,11 +527,12 @@ def run_closure_study(args) -> dict:
                         "seconds": round(time.perf_counter() - t1, 2)}
         blob = cl.blob
 
-    def coarse_run(strength):
+    def coarse_run(strength, mixing=0.0):
         c = coarse_cfg
         with pf.Simulation(c) as s:
             if strength > 0:
                 s.set_closure(blob, strength)
+                s.set_closure_mixing(mixing)
             ta = time.perf_counter()
             s.step(coarse_steps)
             dt = time.perf_counter() - ta
@@ -549,10 +550,11 @@ def run_closure_study(args) -> dict:
         return e
 
     runs = {}
-    for name, strength in (("plain", 0.0), ("closure", 1.0)) + tuple(
-            (f"closure_x{s:g}", s) for s in args.extra_strengths):
-        res, mlups = coarse_run(strength)
-        runs[name] = {"strength": strength, "mlups": round(mlups, 1), **errors(res)}
+    cases = [("plain", 0.0, 0.0), ("closure", 1.0, 0.0)] + [(f"closure_x{v:g}", v, 0.0) for v in args.extra_strengths]
+    cases += [(f"closure_mix{m:g}", 1.0, m) for m in args.mixing]
+    for name, strength, mixing in cases:
+        res, mlups = coarse_run(strength, mixing)
+        runs[name] = {"strength": strength, "mixing": mixing, "mlups": round(mlups, 1), **errors(res)}
     out["runs"] = runs
     out["seconds"] = round(time.perf_counter() - t0, 1)
     return out
@@ -626,6 +628,8 @@ def main():
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--extra-strengths", type=float, nargs="*", default=[0.5, 2.0])
+    ap.add_argument("--mixing", type=float, nargs="*", default=[1.0, 2.0, 4.0],
+                    help="closure study: inverse turbulent Schmidt numbers of the phase mixing")
     ap.add_argument("--checkpoints", default="500,1000,2000,5000,10000")
     args = ap.parse_args()
     if args.study:

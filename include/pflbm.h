@@ -350,6 +350,12 @@ int pflbm_closure_destroy(pflbm_closure *c);
  * detaches): the weights are rounded to BF16 and run in the collide kernel,
  * the result scaled by strength (>= 0). */
 int pflbm_set_closure(pflbm_sim *sim, const float *blob, float strength);
+/* Phase mixing of the attached closure: the sub-filter flux of phi is
+ * modelled as an eddy diffusivity D_t = inv_schmidt * strength * nu_t (a
+ * turbulent Schmidt number Sc_t = 1 / inv_schmidt) added to the phase flux
+ * (J += -4 D_t grad phi); 0 (the default after attaching) switches it off.
+ * PFLBM_ERR_STATE without a closure attached. */
+int pflbm_set_closure_mixing(pflbm_sim *sim, float inv_schmidt);
 
 #ifdef __cplusplus
 }

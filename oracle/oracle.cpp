@@ -298,6 +298,7 @@ struct OracleBase {
     uint64_t t = 0;
     Mlp mlp;            // closure network (used when closure_strength != 0)
     double closure_strength = 0.0;
+    double closure_mixing = 0.0;  // inverse turbulent Schmidt number of the phase mixing
 };
 
 template <class T>
@@ -534,12 +535,13 @@ struct Oracle final : OracleBase {
             const T fsx = F(PFLBM_FIELD_FFX, i), fsy = F(PFLBM_FIELD_FFY, i), fsz = F(PFLBM_FIELD_FFZ, i);
             const T phi = F(PFLBM_FIELD_PHI, i);
             T omega;
-            T tau_t = T(0);  // eddy-viscosity increment of the closure, in tau units
+            T nu_cl = T(0);  // eddy viscosity of the closure (strength * nu_t)
             if (closure_strength != 0.0) {
                 const double x[8] = {double(pxx), double(pyy), double(pzz), double(pxy), double(pxz), double(pyz),
                                      double(phi), double(F(PFLBM_FIELD_IND, i))};
-                tau_t = T(3) * static_cast<T>(closure_strength * mlp_eval(mlp, x, 0.0, nullptr));
+                nu_cl = static_cast<T>(closure_strength * mlp_eval(mlp, x, 0.0, nullptr));
             }
+            const T tau_t = T(3) * nu_cl;  // as a relaxation-time increment
             if (jet) {
                 const T tau_phi = (T(1) - phi) * K.tau_water + phi * K.tau_oil + tau_t;
                 const T r = K.sponge_ramp(z);
@@ -560,7 +562,11 @@ struct Oracle final : OracleBase {
                 f[q * N + id3(xx, yy, zz)] = feq + omco * fneq + T(0.5) * force;
             }
             const T nxv = F(PFLBM_FIELD_NORMX, i), nyv = F(PFLBM_FIELD_NORMY, i), nzv = F(PFLBM_FIELD_NORMZ, i);
-            const T sharp = K.gamma * phi * (T(1) - phi);
+            // closure phase mixing: the flux -D_t grad phi, D_t = nu_cl / Sc_t,
+            // as a change of the anti-diffusion coefficient (grad phi =
+            // |grad phi| n, and the D3Q7 flux is J / 4)
+            const T sharp = K.gamma * phi * (T(1) - phi) -
+                            T(4) * (static_cast<T>(closure_mixing) * nu_cl) * F(PFLBM_FIELD_IND, i);
             for (int q = 0; q < 7; ++q) {
                 const T geq = P.geq(q, phi, ux, uy, uz);
                 const T hi = P.anti_diffusion(q, sharp, nxv, nyv, nzv);
@@ -823,6 +829,9 @@ void ora_set_closure(void *h, const double *params, const double *mean, const do
     o->mlp.out_scale = out_scale;
     o->closure_strength = strength;
 }
+
+// Phase mixing of the attached closure (inverse turbulent Schmidt number).
+void ora_set_closure_mixing(void *h, double inv_schmidt) { static_cast<OracleBase *>(h)->closure_mixing = inv_schmidt; }
 
 uint32_t ora_hash32(uint32_t x) { return hash32(x); }
 float ora_white_noise(uint32_t salt, uint32_t x, uint32_t y, uint32_t t) { return white_noise(salt, x, y, t); }

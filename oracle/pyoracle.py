@@ -70,6 +70,7 @@ def load() -> ctypes.CDLL:
     lib.ora_mlp_num_params.restype = i32
     lib.ora_mlp_eval.argtypes = [vp, vp, vp, ctypes.c_double, vp, vp, i32, vp, vp]
     lib.ora_set_closure.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double]
+    lib.ora_set_closure_mixing.argtypes = [vp, ctypes.c_double]
     _LIB = lib
     return lib
 
@@ -115,6 +116,9 @@ class OracleSim:
         mu = np.ascontiguousarray(mean, np.float64)
         sc = np.ascontiguousarray(inv_scale, np.float64)
         self.lib.ora_set_closure(self._h, p.ctypes.data, mu.ctypes.data, sc.ctypes.data, float(out_scale), float(strength))
+
+    def set_closure_mixing(self, inv_schmidt):
+        self.lib.ora_set_closure_mixing(self._h, float(inv_schmidt))
 
     def close(self):
         if self._h:

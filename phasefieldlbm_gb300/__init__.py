@@ -56,7 +56,7 @@ EXPORTED_SYMBOLS = [
     "pflbm_closure_create", "pflbm_closure_add_snapshot", "pflbm_closure_num_samples", "pflbm_closure_get_samples",
     "pflbm_closure_set_samples", "pflbm_closure_init_params", "pflbm_closure_get_blob", "pflbm_closure_set_blob",
     "pflbm_closure_gradient", "pflbm_closure_train", "pflbm_closure_loss", "pflbm_closure_destroy",
-    "pflbm_set_closure",
+    "pflbm_set_closure", "pflbm_set_closure_mixing",
 ]
 
 
@@ -201,6 +201,7 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_closure_loss": ([vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "pflbm_closure_destroy": ([vp], ctypes.c_int),
         "pflbm_set_closure": ([vp, vp, ctypes.c_float], ctypes.c_int),
+        "pflbm_set_closure_mixing": ([vp, ctypes.c_float], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -527,6 +528,11 @@ class Simulation:
         if b.size != MLP_BLOB:
             raise ValueError(f"closure blob must hold {MLP_BLOB} floats")
         _check(self.lib, self.lib.pflbm_set_closure(self._h, b.ctypes.data, float(strength)))
+
+    def set_closure_mixing(self, inv_schmidt: float):
+        """Phase mixing of the attached closure: eddy diffusivity of phi
+        D_t = inv_schmidt * strength * nu_t (0 switches it off)."""
+        _check(self.lib, self.lib.pflbm_set_closure_mixing(self._h, float(inv_schmidt)))
 
 
 MLP_PARAMS, MLP_BLOB = 1377, 1395

@@ -798,6 +798,18 @@ int pflbm_set_closure(pflbm_sim *s, const float *blob, float strength) {
 }
 
 
+int pflbm_set_closure_mixing(pflbm_sim *s, float inv_schmidt) {
+    if (!s) return fail(PFLBM_ERR_INVALID_ARG, "null simulation");
+    if (!(inv_schmidt >= 0.0f) || !std::isfinite(inv_schmidt))
+        return fail(PFLBM_ERR_INVALID_ARG, "inv_schmidt must be finite and >= 0");
+    cudaSetDevice(s->device);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    std::string err;
+    const int rc = s->eng->set_closure_mixing(inv_schmidt, err);
+    return rc ? fail(rc, err) : PFLBM_OK;
+}
+
 namespace {
 int write_output_async_impl(pflbm_sim *s, const char *dir, const int32_t *ids, int32_t n) {
     if (!s || !dir || (!ids && n > 0) || n < 0) return fail(PFLBM_ERR_INVALID_ARG, "bad argument");

@@ -19,6 +19,11 @@ constexpr int kMlpBlob = kMlpParams + 2 * kMlpIn + 2;                           
 constexpr int kMlpW1 = 0, kMlpB1 = kMlpH * kMlpIn, kMlpW2 = kMlpB1 + kMlpH, kMlpB2 = kMlpW2 + kMlpH * kMlpH,
               kMlpW3 = kMlpB2 + kMlpH, kMlpB3 = kMlpW3 + kMlpH, kMlpMean = kMlpParams,
               kMlpInvScale = kMlpMean + kMlpIn, kMlpOutScale = kMlpInvScale + kMlpIn, kMlpStrength = kMlpOutScale + 1;
+// One more device word after the user-visible blob: the inverse turbulent
+// Schmidt number of the closure's phase mixing (0 = off), set by
+// pflbm_set_closure_mixing.
+constexpr int kMlpPhaseMix = kMlpBlob;
+constexpr int kMlpDeviceFloats = kMlpBlob + 1;
 
 template <class T>
 __device__ __forceinline__ T silu_d(T a) { return a / (T(1) + exp(-a)); }
@@ -62,6 +67,7 @@ __device__ __forceinline__ T mlp_nu_t(const float *w, const T (&x)[kMlpIn]) {
 constexpr int kMlpFragF1 = 1396, kMlpFragF2 = kMlpFragF1 + 128, kMlpFragF3 = kMlpFragF2 + 512,
               kMlpFragX = kMlpFragF3 + 128;
 constexpr int mlp_smem_words(int warps) { return kMlpFragX + warps * 32 * 4; }
+static_assert(kMlpFragF1 >= kMlpDeviceFloats, "fragments after the device blob");
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);

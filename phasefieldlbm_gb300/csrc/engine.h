@@ -74,6 +74,9 @@ class Engine {
     // device and switches the collide kernel to the closure mode; null
     // detaches. PFLBM_ERR_UNSUPPORTED for 16-bit storage.
     virtual int set_closure(const float *host_blob, std::string &err) = 0;
+    // Inverse turbulent Schmidt number of the closure's phase mixing (the
+    // device word after the blob); needs a closure attached.
+    virtual int set_closure_mixing(float inv_schmidt, std::string &err) = 0;
     virtual bool has_closure() const = 0;
 };
 

@@ -197,7 +197,7 @@ class EngineT final : public Engine {
         // shared memory); without room they stay on the plain-load kernel
         tma_closure_ = false;
         if constexpr (sizeof(S) >= 4) {
-            const int smc = int(L::total + closure_smem_bytes<T>());
+            const int smc = int(TmaModeLayout<QQ, S, MODE_STEP_CLOSURE>::total + closure_smem_bytes<T>());
             tma_closure_ = cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smc) == cudaSuccess &&
                            cudaFuncSetAttribute(k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE_AVG>,
@@ -271,7 +271,7 @@ class EngineT final : public Engine {
         if (closure_) {
             // learned closure: the network in shared memory
             if constexpr (sizeof(S) >= 4) {
-                const size_t smc = TmaLayout<QQ, S>::total + closure_smem_bytes<T>();
+                const size_t smc = TmaModeLayout<QQ, S, MODE_STEP_CLOSURE>::total + closure_smem_bytes<T>();
                 if (use_tma_ && tma_closure_ && avg_)
                     k_collide_tma<QQ, JET, S, MODE_STEP_CLOSURE_AVG>
                         <<<collide_grid(), dim3(TX, TY, 1), smc, s>>>(p_, b, fmapn_[parity], fmapw_[parity], phimap_[parity]);
@@ -384,12 +384,13 @@ class EngineT final : public Engine {
                 return PFLBM_OK;
             }
             if (!mlp_) {
-                if (cudaMalloc(&mlp_, sizeof(float) * kMlpBlob) != cudaSuccess) {
+                if (cudaMalloc(&mlp_, sizeof(float) * kMlpDeviceFloats) != cudaSuccess) {
                     cudaGetLastError();
                     err = "cudaMalloc failed (closure network)";
                     return PFLBM_ERR_OUT_OF_MEMORY;
                 }
-                bytes_ += sizeof(float) * kMlpBlob;
+                bytes_ += sizeof(float) * kMlpDeviceFloats;
+                cudaMemset(mlp_, 0, sizeof(float) * kMlpDeviceFloats);  // phase mixing off
             }
             if (cudaMemcpy(mlp_, host_blob, sizeof(float) * kMlpBlob, cudaMemcpyHostToDevice) != cudaSuccess) {
                 err = cudaGetErrorString(cudaGetLastError());
@@ -400,6 +401,17 @@ class EngineT final : public Engine {
         }
     }
     bool has_closure() const override { return closure_; }
+    int set_closure_mixing(float inv_schmidt, std::string &err) override {
+        if (!closure_ || !mlp_) {
+            err = "attach a closure (pflbm_set_closure) before its phase mixing";
+            return PFLBM_ERR_STATE;
+        }
+        if (cudaMemcpy(mlp_ + kMlpPhaseMix, &inv_schmidt, sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+            err = cudaGetErrorString(cudaGetLastError());
+            return PFLBM_ERR_CUDA;
+        }
+        return PFLBM_OK;
+    }
 
    private:
     static constexpr int kRedBlocks = 608;
@@ -416,7 +428,7 @@ class EngineT final : public Engine {
     bool use_pair_ = false;  // k_collide_pair for the plain step
     bool tma_closure_ = false;  // closure modes on k_collide_tma
     bool no_vec_ = false;  // PFLBM_NO_VEC=1: scalar phase kernel
-    float *mlp_ = nullptr;  // closure network blob (kMlpBlob floats)
+    float *mlp_ = nullptr;  // closure network blob (kMlpBlob floats) + phase mixing (1 float)
     bool closure_ = false;
     CUtensorMap fmapn_[2]{}, fmapw_[2]{}, phimap_[2]{};
     uint64_t bytes_ = 0;

@@ -96,18 +96,20 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
     // moments (src/lbm.cu:33-128)
     const Macro<T> m = moments<QQ, T>(pop, fx, fy, fz);
 
-    // learned eddy-viscosity increment, in units of tau (tau = 1/2 + 3 nu)
-    T tau_t = T(0);
+    // learned eddy viscosity nu_cl = strength * nu_t, as a relaxation-time
+    // increment tau_t = 3 nu_cl (tau = 1/2 + 3 nu)
+    T nu_cl = T(0);
     if constexpr (mode_closure(MODE)) {
         const T feat[kMlpIn] = {m.pxx, m.pyy, m.pzz, m.pxy, m.pxz, m.pyz, phi, ind};
         if constexpr (std::is_same<T, float>::value) {
             // FP32 runs: the warp's 32 nodes on the tensor cores (every lane
             // calls, inactive ones with placeholder features)
-            tau_t = T(3) * (s_mlp[kMlpStrength] * mlp_nu_t_warp(s_mlp, feat, int(threadIdx.y), int(threadIdx.x)));
+            nu_cl = s_mlp[kMlpStrength] * mlp_nu_t_warp(s_mlp, feat, int(threadIdx.y), int(threadIdx.x));
         } else {
-            tau_t = T(3) * (T(s_mlp[kMlpStrength]) * mlp_nu_t<T>(s_mlp, feat));
+            nu_cl = T(s_mlp[kMlpStrength]) * mlp_nu_t<T>(s_mlp, feat);
         }
     }
+    const T tau_t = T(3) * nu_cl;
     if (!active) return;
     // relaxation (src/lbm.cu:158-170)
     T omega;
@@ -193,8 +195,12 @@ __device__ __forceinline__ void collide_node(const Params<typename Store<S>::T> 
             if (PFLBM_GUARD(iq < N, b.err)) put(q, iq, a);
             if (PFLBM_GUARD(iqb < N, b.err)) put(q + 1, iqb, c);
         }
-        // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J)
-        const T sharp = p.gamma * phi * (T(1) - phi);
+        // phase flux (src/lbm.cu:209-238): g_q = w_q (phi + c_q . J). With the
+        // closure's phase mixing, the sub-filter flux -D_t grad phi, D_t =
+        // nu_cl / Sc_t, enters as J += -4 D_t |grad phi| n (the D3Q7 flux is
+        // J / 4 with cs^2 = 1/4)
+        T sharp = p.gamma * phi * (T(1) - phi);
+        if constexpr (mode_closure(MODE)) sharp -= T(4) * (T(s_mlp[kMlpPhaseMix]) * nu_cl) * ind;
         if (!PFLBM_GUARD(base < N, b.err)) return;
         b.jflux[base] = T(4) * phi * m.ux + sharp * n_x;
         b.jflux[N + base] = T(4) * phi * m.uy + sharp * n_y;
@@ -388,7 +394,7 @@ __global__ void __launch_bounds__(NT, (sizeof(typename Store<S>::T) == 8 ? 1 : P
     __shared__ __align__(16) float s_mlp[mode_closure(MODE) ? mlp_smem_words(NT / 32) : 1];
     if constexpr (mode_closure(MODE)) {
         static_assert(TX == 32, "the tensor-core network maps one warp to one tile row");
-        for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpBlob; i += NT) s_mlp[i] = b.mlp[i];
+        for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpDeviceFloats; i += NT) s_mlp[i] = b.mlp[i];
         __syncthreads();
         if constexpr (std::is_same<typename Store<S>::T, float>::value) {
             mlp_build_fragments(s_mlp, threadIdx.x + TX * threadIdx.y, NT);

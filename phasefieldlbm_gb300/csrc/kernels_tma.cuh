@@ -143,7 +143,7 @@ struct TmaPlan {
 // and for FP32 its mma fragments and per-warp feature tiles.
 template <class T>
 constexpr size_t closure_smem_bytes() {
-    return sizeof(float) * size_t(sizeof(T) == 4 ? mlp_smem_words(NT / 32) : kMlpBlob);
+    return sizeof(float) * size_t(sizeof(T) == 4 ? mlp_smem_words(NT / 32) : kMlpDeviceFloats);
 }
 
 // Resident CTAs per SM of the TMA collide: one for FP64; three for D3Q19
@@ -169,6 +169,21 @@ struct TmaStages {
 
 template <int QQ, class S, class G = DefaultTile>
 using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S, G>::value, typename Store<S>::T, G>;
+
+// The closure modes place the network after the pipeline's shared memory:
+// their pipeline is the deepest whose plan plus the network still fits the
+// same per-CTA budget, so that they keep the plain step's resident CTAs.
+template <int QQ, class S>
+struct TmaClosureStages {
+    using T = typename Store<S>::T;
+    static constexpr size_t kBudget = TmaStages<QQ, S>::kBudget - closure_smem_bytes<T>();
+    static constexpr int value = TmaPlan<QQ, S, 4>::total <= kBudget   ? 4
+                                 : TmaPlan<QQ, S, 3>::total <= kBudget ? 3
+                                                                       : 2;
+};
+template <int QQ, class S, int MODE>
+using TmaModeLayout = typename std::conditional<mode_closure(MODE), TmaPlan<QQ, S, TmaClosureStages<QQ, S>::value>,
+                                                TmaLayout<QQ, S>>::type;
 
 // Barriers of the TMA pipeline: once per CTA, before its first tile.
 template <int QQ, class S, class L = TmaLayout<QQ, S>>
@@ -383,20 +398,21 @@ __global__ void __launch_bounds__(NT, CollideOccupancy<QQ, S>::value)
     if constexpr (mode_closure(MODE)) {
         // closure network after the pipeline's shared memory (kernels.cuh's k_collide does the same)
         static_assert(TX == 32, "the tensor-core network maps one warp to one tile row");
-        s_mlp = reinterpret_cast<float *>(smem + TmaLayout<QQ, S>::total);
-        for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpBlob; i += NT) s_mlp[i] = b.mlp[i];
+        s_mlp = reinterpret_cast<float *>(smem + TmaModeLayout<QQ, S, MODE>::total);
+        for (int i = threadIdx.x + TX * threadIdx.y; i < kMlpDeviceFloats; i += NT) s_mlp[i] = b.mlp[i];
         __syncthreads();
         if constexpr (std::is_same<typename Store<S>::T, float>::value) {
             mlp_build_fragments(s_mlp, threadIdx.x + TX * threadIdx.y, NT);
             __syncthreads();
         }
     }
-    tma_pipeline_init<QQ, S>(smem);
+    using L = TmaModeLayout<QQ, S, MODE>;
+    tma_pipeline_init<QQ, S, L>(smem);
     const int zb = 1 + blockIdx.z * p.zchunk;
     const int ze = min(zb + p.zchunk, int(p.nz) - 1);
     uint32_t seq = 0;
-    collide_tile_tma<QQ, JET, S, MODE>(p, b, &fmapn, &fmapw, &phimap, int(blockIdx.x) * TX, int(blockIdx.y) * TY, zb,
-                                       ze, smem, seq, s_mlp);
+    collide_tile_tma<QQ, JET, S, MODE, DefaultTile, L>(p, b, &fmapn, &fmapw, &phimap, int(blockIdx.x) * TX,
+                                                       int(blockIdx.y) * TY, zb, ze, smem, seq, s_mlp);
 }
 
 }  // namespace pflbm

@@ -68,7 +68,11 @@ def test_training_fits_a_known_closure(pflbm):
     assert l1 < l0 / 20
 
 
-def test_closure_collision_matches_oracle(pflbm, oracle):
+@pytest.mark.parametrize("mixing", [0.0, 2.0])
+def test_closure_collision_matches_oracle(pflbm, oracle, mixing):
+    """The closure-coupled collision (and, with mixing > 0, the closure's
+    phase mixing D_t = mixing * nu_t in the phase flux) of an FP64 jet
+    against the FP64 oracle with the same BF16-rounded network: <= 1e-10."""
     cfg = pflbm.config_reference(pflbm.CASE_JET, pflbm.VS_D3Q19)
     cfg.nx, cfg.ny, cfg.nz, cfg.diam, cfg.radius = 24, 24, 36, 8, 4
     cfg.storage = pflbm.STORAGE_FP64
@@ -84,6 +88,7 @@ def test_closure_collision_matches_oracle(pflbm, oracle):
     steps = 20
     with pflbm.Simulation(cfg) as s:
         s.set_closure(blob, strength=1.0)
+        s.set_closure_mixing(mixing)
         s.step(steps)
         lib = {f: s.get_field(f, dtype=np.float64) for f in ("rho", "ux", "uy", "uz", "phi")}
     with pflbm.Simulation(cfg) as s:
@@ -92,6 +97,7 @@ def test_closure_collision_matches_oracle(pflbm, oracle):
     p, mu, sc, osc = _split(blob.astype(np.float64))
     o = oracle.OracleSim(cfg, fp64=True)
     o.set_closure(pflbm.bf16_round(blob[:1377]).astype(np.float64), mu, sc, osc, 1.0)
+    o.set_closure_mixing(mixing)
     o.step(steps)
     for f in lib:
         assert rel_l2(lib[f], o.get_field(f)) <= 1e-10, f
@@ -251,7 +257,9 @@ def test_trained_closure_beats_constant_tau(pflbm):
     """The learned part end to end at a small scale: snapshots of a 2x-finer
     run of the same seeded jet (Re = 10000), GPU training, then coarse runs
     with and without the closure judged by the relative L2 error of their
-    time-averaged u_z and phi against the filtered fine average."""
+    time-averaged u_z and phi against the filtered fine average: the closure
+    must lower both errors (measured 0.447 -> 0.387 on <u_z>, 0.2276 ->
+    0.2258 on <phi>)."""
     fine_cfg, coarse_cfg = _jet_closure_pair(pflbm, 96, 384, 12)
     snaps, every = 10, 200
     with pflbm.Closure(2_000_000) as cl:
@@ -276,7 +284,7 @@ def test_trained_closure_beats_constant_tau(pflbm):
             err[name] = {f: rel_l2(s.get_field(f).astype(np.float64)[sl], ref[f][sl]) for f in ("avg_uz", "avg_phi")}
     print("training loss", l0, "->", l1, "errors", err)
     assert err["closure"]["avg_uz"] < err["plain"]["avg_uz"]
-    assert err["closure"]["avg_phi"] < 1.01 * err["plain"]["avg_phi"]
+    assert err["closure"]["avg_phi"] < err["plain"]["avg_phi"]
 
 
 @pytest.mark.parametrize("storage,avg", [(0, 0), (0, 1), (3, 0)])
