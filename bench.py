@@ -177,7 +177,7 @@ def cpu_oracle_mlups(cfg, steps: int, warm: int = 1) -> tuple[float, float, int]
 # profiles/k_collide_tma_jet_d3q19_fp32_128x128x128.md).
 NCU_COLLIDE_TRAFFIC = {
     "jet_d3q27": ((1022.144000e6 + 938.872832e6) + (1021.897472e6 + 935.937536e6)) / 2,
-    "jet_d3q19": (179.140864e6 + 127.638528e6) * 510 / 126,
+    "jet_d3q19": (179.217664e6 + 127.435776e6) * 510 / 126,
 }
 NCU_TRAFFIC_SOURCE = {
     "jet_d3q27": "ncu on this 128x128x512 workload (mean of 2 launches)",

@@ -172,9 +172,18 @@ def test_derived_fields_match_oracle(pflbm, oracle):
             assert rel_l2(s.get_field(f, dtype=np.float64), o.get_field(f)) <= 1e-10, f
 
 
+# 16-bit storage against FP32 storage on the same young jet (60 steps,
+# reference physics): rel. L2 bounds about 2-5x the measured FP16 (rho
+# 3.9e-7, u 3.8e-4, phi 7.3e-6) and BF16 (rho 4.4e-6, u 4.4e-3, phi 1.2e-4)
+# differences
+LOW_PRECISION_TOL = {
+    1: {"rho": 2e-6, "ux": 1e-3, "uy": 1e-3, "uz": 5e-4, "phi": 3e-5},
+    2: {"rho": 2e-5, "ux": 1e-2, "uy": 1e-2, "uz": 5e-3, "phi": 5e-4},
+}
+
+
 def test_low_precision_storage_close_to_fp32(pflbm):
     c = jet_cfg(pflbm, 19, nx=32, ny=32, nz=48, diam=8)
-    ref = {}
     with pflbm.Simulation(c) as s:
         s.step(60)
         ref = {f: s.get_field(f) for f in BASIC}
@@ -183,9 +192,10 @@ def test_low_precision_storage_close_to_fp32(pflbm):
         c2.storage = st
         with pflbm.Simulation(c2) as s:
             s.step(60)
-            assert rel_l2(s.get_field("rho"), ref["rho"]) < 1e-4
-            assert rel_l2(s.get_field("phi"), ref["phi"]) < 2e-2
-            assert rel_l2(s.get_field("uz"), ref["uz"]) < 5e-2
+            e = {f: rel_l2(s.get_field(f), ref[f]) for f in BASIC}
+        print("storage", st, e)
+        bad = {f: v for f, v in e.items() if not v <= LOW_PRECISION_TOL[st][f]}
+        assert not bad, (st, bad, e)
 
 
 def test_write_output_layout(pflbm, tmp_path):
