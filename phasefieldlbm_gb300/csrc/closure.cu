@@ -25,6 +25,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -289,6 +290,264 @@ __global__ void __launch_bounds__(kSB) k_mlp_grad(const float *__restrict__ blob
     }
 }
 
+// ------------------------------------------- network on the tensor cores
+// The same forward + backward over kSB = 128 samples per CTA with every
+// matrix product on the tensor cores: warp-level mma.m16n8k8 with TF32
+// operands (10-bit mantissa, operands rounded to nearest) and FP32
+// accumulation. Warp w owns samples 32w .. 32w+31 (two 16-row tiles):
+//   layer 1   A1 = Xn W1^T + b1       (16 x 8 x 8 per tile and column block)
+//   layer 2   A2 = H1 W2^T + b2       (K = 32: four k steps)
+//   backward  dH1 = dA2 W2            (K = 32)
+//   weights   dW2 = dA2^T H1, dW1 = dA1^T Xn   (K = the warp's 32 samples)
+// and the elementwise parts (SiLU, softplus, bias and w3 sums) in FP32. The
+// four warps' partial gradients are summed in warp order: gpart is filled
+// as k_mlp_grad fills it (sums over the CTA's samples, loss last).
+constexpr int kTcWarps = kSB / 32;
+constexpr int kTcX = 12;                 // row stride of the Xn tile (floats)
+constexpr int kTcH = kMlpH + 4;          // row stride of the 32-wide tiles
+constexpr int kTcWarpFloats = 32 * kTcX + 3 * 32 * kTcH + 32;  // Xn, H1, dA2, dA1, dz
+constexpr int kTcPart = kMlpParams + 1;  // per-warp partial gradient + loss
+
+size_t tc_smem_bytes() {
+    return sizeof(float) * (size_t(kMlpBlob) + size_t(kTcWarps) * kTcWarpFloats + size_t(kTcWarps) * kTcPart);
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+// D = A B + C, A 16x8 (row), B 8x8 (col), TF32 operands, FP32 accumulators.
+__device__ __forceinline__ void mma_tf32_1688(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                              uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float silu_grad(float a) {
+    const float sg = sigmoidf_(a);
+    return sg * (1.0f + a * (1.0f - sg));
+}
+
+__global__ void __launch_bounds__(kSB) k_mlp_grad_tc(const float *__restrict__ blob, const float *__restrict__ X,
+                                                     const float *__restrict__ Y, uint64_t n, int mode,
+                                                     uint64_t seed, uint64_t iter, uint64_t count,
+                                                     float *__restrict__ gpart) {
+    extern __shared__ float tcs[];
+    float *w = tcs;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    float *base = tcs + kMlpBlob + warp * kTcWarpFloats;
+    float *xs = base;                       // [32][kTcX]
+    float *h1s = xs + 32 * kTcX;            // [32][kTcH]
+    float *da2s = h1s + 32 * kTcH;          // [32][kTcH]
+    float *da1s = da2s + 32 * kTcH;         // [32][kTcH]
+    float *dzs = da1s + 32 * kTcH;          // [32]
+    float *part = tcs + kMlpBlob + kTcWarps * kTcWarpFloats + warp * kTcPart;
+    for (int i = threadIdx.x; i < kMlpBlob; i += kSB) w[i] = blob[i];
+    __syncthreads();
+    const float out_scale = w[pflbm::kMlpOutScale];
+
+    // this lane's sample (row `lane` of the warp's tile): normalised features
+    const uint64_t k = blockIdx.x * uint64_t(kSB) + threadIdx.x;
+    const bool valid = k < count;
+    uint64_t idx = 0;
+    if (valid) idx = mode == 0 ? k : mix64(seed * 0x9E3779B97F4A7C15ull + mix64(iter * 0x100000001B3ull + k)) % n;
+    for (int q = 0; q < kMlpIn; ++q)
+        xs[lane * kTcX + q] = valid ? (X[idx * kMlpIn + q] - w[pflbm::kMlpMean + q]) * w[pflbm::kMlpInvScale + q]
+                                    : 0.0f;
+    const float target = valid ? Y[idx] / out_scale : 0.0f;
+    __syncwarp();
+
+    // layer 1: a1 = Xn W1^T + b1 (fragments: rows 16 mt + g (+8), columns
+    // 8 nt + 2 t (+1)); h1 = SiLU(a1) to shared memory
+    float a1[2][4][4], a2[2][4][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            float(&d)[4] = a1[mt][nt];
+            d[0] = d[2] = w[pflbm::kMlpB1 + 8 * nt + 2 * t];
+            d[1] = d[3] = w[pflbm::kMlpB1 + 8 * nt + 2 * t + 1];
+            const int r0 = 16 * mt + g;
+            mma_tf32_1688(d, to_tf32(xs[r0 * kTcX + t]), to_tf32(xs[(r0 + 8) * kTcX + t]),
+                          to_tf32(xs[r0 * kTcX + t + 4]), to_tf32(xs[(r0 + 8) * kTcX + t + 4]),
+                          to_tf32(w[pflbm::kMlpW1 + (8 * nt + g) * kMlpIn + t]),
+                          to_tf32(w[pflbm::kMlpW1 + (8 * nt + g) * kMlpIn + t + 4]));
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int row = r0 + (e >= 2 ? 8 : 0), col = 8 * nt + 2 * t + (e & 1);
+                h1s[row * kTcH + col] = d[e] * sigmoidf_(d[e]);
+            }
+        }
+    __syncwarp();
+    // layer 2: a2 = H1 W2^T + b2; z = w3 . SiLU(a2) + b3 per sample
+    float zp[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [mt][row g / g + 8], this lane's columns
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            float(&d)[4] = a2[mt][nt];
+            d[0] = d[2] = w[pflbm::kMlpB2 + 8 * nt + 2 * t];
+            d[1] = d[3] = w[pflbm::kMlpB2 + 8 * nt + 2 * t + 1];
+            const int r0 = 16 * mt + g;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                mma_tf32_1688(d, to_tf32(h1s[r0 * kTcH + 8 * kk + t]), to_tf32(h1s[(r0 + 8) * kTcH + 8 * kk + t]),
+                              to_tf32(h1s[r0 * kTcH + 8 * kk + t + 4]),
+                              to_tf32(h1s[(r0 + 8) * kTcH + 8 * kk + t + 4]),
+                              to_tf32(w[pflbm::kMlpW2 + (8 * nt + g) * kMlpH + 8 * kk + t]),
+                              to_tf32(w[pflbm::kMlpW2 + (8 * nt + g) * kMlpH + 8 * kk + t + 4]));
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int col = 8 * nt + 2 * t + (e & 1);
+                zp[mt][e >> 1] += w[pflbm::kMlpW3 + col] * (d[e] * sigmoidf_(d[e]));
+            }
+        }
+    // complete z over the 4 lanes of a group, then dz per row to shared memory
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            zp[mt][h] += __shfl_xor_sync(0xffffffffu, zp[mt][h], 1);
+            zp[mt][h] += __shfl_xor_sync(0xffffffffu, zp[mt][h], 2);
+        }
+    if (t == 0) {
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) dzs[16 * mt + g + 8 * h] = zp[mt][h] + w[pflbm::kMlpB3];
+    }
+    __syncwarp();
+    // this lane's own sample: loss and dz
+    float loss_l, dz_l;
+    {
+        const float z = dzs[lane];
+        const float sp = fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z)));
+        const float r = valid ? sp - target : 0.0f;
+        loss_l = valid ? r * r : 0.0f;
+        dz_l = valid ? 2.0f * r * sigmoidf_(z) : 0.0f;
+    }
+    __syncwarp();
+    dzs[lane] = dz_l;
+    __syncwarp();
+    // backward: dA2 = dz w3 SiLU'(a2); dw3 partials over this lane's rows
+    float dw3p[4][2] = {};
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int row = 16 * mt + g + (e >= 2 ? 8 : 0), col = 8 * nt + 2 * t + (e & 1);
+                const float dz = dzs[row], av = a2[mt][nt][e];
+                da2s[row * kTcH + col] = dz * w[pflbm::kMlpW3 + col] * silu_grad(av);
+                dw3p[nt][e & 1] += dz * (av * sigmoidf_(av));
+            }
+    __syncwarp();
+    // dH1 = dA2 W2, dA1 = dH1 SiLU'(a1)
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
+            const int r0 = 16 * mt + g;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                mma_tf32_1688(d, to_tf32(da2s[r0 * kTcH + 8 * kk + t]), to_tf32(da2s[(r0 + 8) * kTcH + 8 * kk + t]),
+                              to_tf32(da2s[r0 * kTcH + 8 * kk + t + 4]),
+                              to_tf32(da2s[(r0 + 8) * kTcH + 8 * kk + t + 4]),
+                              to_tf32(w[pflbm::kMlpW2 + (8 * kk + t) * kMlpH + 8 * nt + g]),
+                              to_tf32(w[pflbm::kMlpW2 + (8 * kk + t + 4) * kMlpH + 8 * nt + g]));
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int row = r0 + (e >= 2 ? 8 : 0), col = 8 * nt + 2 * t + (e & 1);
+                da1s[row * kTcH + col] = d[e] * silu_grad(a1[mt][nt][e]);
+            }
+        }
+    __syncwarp();
+    // weight gradients over the warp's 32 samples (K)
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {  // dW2[j][i] = sum_s dA2[s][j] H1[s][i]
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                mma_tf32_1688(d, to_tf32(da2s[(8 * kk + t) * kTcH + 16 * mt + g]),
+                              to_tf32(da2s[(8 * kk + t) * kTcH + 16 * mt + g + 8]),
+                              to_tf32(da2s[(8 * kk + t + 4) * kTcH + 16 * mt + g]),
+                              to_tf32(da2s[(8 * kk + t + 4) * kTcH + 16 * mt + g + 8]),
+                              to_tf32(h1s[(8 * kk + t) * kTcH + 8 * nt + g]),
+                              to_tf32(h1s[(8 * kk + t + 4) * kTcH + 8 * nt + g]));
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int j = 16 * mt + g + (e >= 2 ? 8 : 0), i = 8 * nt + 2 * t + (e & 1);
+                part[pflbm::kMlpW2 + j * kMlpH + i] = d[e];
+            }
+        }
+        float d[4] = {0.f, 0.f, 0.f, 0.f};  // dW1[i][q] = sum_s dA1[s][i] Xn[s][q]
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+            mma_tf32_1688(d, to_tf32(da1s[(8 * kk + t) * kTcH + 16 * mt + g]),
+                          to_tf32(da1s[(8 * kk + t) * kTcH + 16 * mt + g + 8]),
+                          to_tf32(da1s[(8 * kk + t + 4) * kTcH + 16 * mt + g]),
+                          to_tf32(da1s[(8 * kk + t + 4) * kTcH + 16 * mt + g + 8]),
+                          to_tf32(xs[(8 * kk + t) * kTcX + g]), to_tf32(xs[(8 * kk + t + 4) * kTcX + g]));
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int i = 16 * mt + g + (e >= 2 ? 8 : 0), q = 2 * t + (e & 1);
+            part[pflbm::kMlpW1 + i * kMlpIn + q] = d[e];
+        }
+    }
+    // bias and w3 gradients, loss: column sums over the warp's samples
+    {
+        float sb1 = 0.f, sb2 = 0.f;
+        for (int s = 0; s < 32; ++s) {
+            sb1 += da1s[s * kTcH + lane];
+            sb2 += da2s[s * kTcH + lane];
+        }
+        part[pflbm::kMlpB1 + lane] = sb1;
+        part[pflbm::kMlpB2 + lane] = sb2;
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            float v = dw3p[nt][c];
+            v += __shfl_xor_sync(0xffffffffu, v, 4);
+            v += __shfl_xor_sync(0xffffffffu, v, 8);
+            v += __shfl_xor_sync(0xffffffffu, v, 16);
+            if (g == 0) part[pflbm::kMlpW3 + 8 * nt + 2 * t + c] = v;
+        }
+    {
+        float sdz = dz_l, sl = loss_l;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sdz += __shfl_xor_sync(0xffffffffu, sdz, o);
+            sl += __shfl_xor_sync(0xffffffffu, sl, o);
+        }
+        if (lane == 0) {
+            part[pflbm::kMlpB3] = sdz;
+            part[kMlpParams] = sl;
+        }
+    }
+    __syncthreads();
+    // the block's sums, warps in order
+    float *gout = gpart + size_t(blockIdx.x) * (kMlpParams + 1);
+    const float *parts = tcs + kMlpBlob + kTcWarps * kTcWarpFloats;
+    for (int p = threadIdx.x; p <= kMlpParams; p += kSB) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int ww = 0; ww < kTcWarps; ++ww) acc += parts[ww * kTcPart + p];
+        gout[p] = acc;
+    }
+}
+
 // Sums the block gradients (fixed order, FP64) into grad[0..kMlpParams]
 // (the last entry is the loss sum).
 __global__ void k_grad_sum(const float *__restrict__ gpart, int nblocks, double *__restrict__ grad) {
@@ -400,6 +659,23 @@ int download_blob(pflbm_closure *c) {
 
 size_t act_bytes() { return sizeof(Act); }
 
+// Gradient kernel of a training step: the tensor-core kernel, or with
+// PFLBM_MLP_SIMT=1 the FP32 CUDA-core kernel (exact FP32 products, for
+// checks against the FP64 oracle at FP32 rounding).
+bool use_simt_grad() {
+    const char *e = std::getenv("PFLBM_MLP_SIMT");
+    return e && e[0] == '1';
+}
+
+void launch_grad(pflbm_closure *c, int blocks, int mode, uint64_t seed, uint64_t iter, uint64_t count) {
+    if (use_simt_grad())
+        k_mlp_grad<<<blocks, kSB, act_bytes(), c->stream>>>(c->blob, c->X, c->Y, c->n, mode, seed, iter, count,
+                                                            c->gpart);
+    else
+        k_mlp_grad_tc<<<blocks, kSB, tc_smem_bytes(), c->stream>>>(c->blob, c->X, c->Y, c->n, mode, seed, iter,
+                                                                   count, c->gpart);
+}
+
 }  // namespace
 
 extern "C" {
@@ -432,6 +708,9 @@ int pflbm_closure_create(int32_t device, uint64_t max_samples, pflbm_closure **o
     }
     if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, int(act_bytes())) != cudaSuccess)
         return cuda_fail(cudaGetLastError(), "k_mlp_grad shared memory");
+    if (cudaFuncSetAttribute(k_mlp_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc_smem_bytes())) !=
+        cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "k_mlp_grad_tc shared memory");
     *out = c.release();
     return PFLBM_OK;
 }
@@ -583,7 +862,7 @@ int pflbm_closure_gradient(pflbm_closure *c, uint64_t count, double *host_grad, 
     cudaSetDevice(c->device);
     const int blocks = int((count + kSB - 1) / kSB);
     if (int rc = ensure_gpart(c, blocks)) return rc;
-    k_mlp_grad<<<blocks, kSB, act_bytes(), c->stream>>>(c->blob, c->X, c->Y, c->n, 0, 0, 0, count, c->gpart);
+    launch_grad(c, blocks, 0, 0, 0, count);
     k_grad_sum<<<(kMlpParams + 1 + 255) / 256, 256, 0, c->stream>>>(c->gpart, blocks, c->grad);
     std::vector<double> g(kMlpParams + 1);
     cudaError_t e = cudaMemcpyAsync(g.data(), c->grad, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, c->stream);
@@ -617,8 +896,7 @@ int pflbm_closure_train(pflbm_closure *c, int32_t iterations, int32_t batch, flo
         const uint64_t t = ++c->adam_t;
         const float c1 = float(1.0 - std::pow(double(beta1), double(t)));
         const float c2 = float(1.0 - std::pow(double(beta2), double(t)));
-        k_mlp_grad<<<blocks, kSB, act_bytes(), c->stream>>>(c->blob, c->X, c->Y, c->n, 1, seed, t, uint64_t(batch),
-                                                            c->gpart);
+        launch_grad(c, blocks, 1, seed, t, uint64_t(batch));
         k_adam<<<(kMlpParams + 1 + 255) / 256, 256, 0, c->stream>>>(c->blob, c->m, c->v, c->gpart, blocks,
                                                                    1.0f / float(batch), lr, beta1, beta2, eps, c1, c2,
                                                                    c->loss_log, it);

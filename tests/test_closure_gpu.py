@@ -30,7 +30,16 @@ def _split(blob):
     return blob[:1377], blob[1377:1385], blob[1385:1393], float(blob[1393])
 
 
-def test_gradient_matches_oracle(pflbm, oracle):
+# Gradient of the training loss against the FP64 oracle (rel. L2, every
+# layer): the FP32 CUDA-core kernel (PFLBM_MLP_SIMT=1) at FP32 rounding,
+# 1e-4; the default tensor-core kernel (TF32 operands: 10-bit mantissa,
+# relative rounding 2^-11 per operand) at 1e-3 (measured 2.3e-4).
+@pytest.mark.parametrize("kernel,tol", [("simt", 1e-4), ("tensor", 1e-3)])
+def test_gradient_matches_oracle(pflbm, oracle, monkeypatch, kernel, tol):
+    if kernel == "simt":
+        monkeypatch.setenv("PFLBM_MLP_SIMT", "1")
+    else:
+        monkeypatch.delenv("PFLBM_MLP_SIMT", raising=False)
     n = 300  # not a multiple of the 128-sample block
     x = _features(n, 1)
     y = np.abs(np.random.default_rng(2).normal(2e-4, 1e-4, n))
@@ -46,10 +55,13 @@ def test_gradient_matches_oracle(pflbm, oracle):
     out, g_ref = oracle.mlp_eval(p, mu, sc, osc, x.astype(np.float32).astype(np.float64),
                                  y.astype(np.float32).astype(np.float64), with_grad=True)
     loss_ref = float(np.sum((out / osc - y.astype(np.float32) / osc) ** 2))
-    assert rel_l2(g, g_ref) <= 1e-4, rel_l2(g, g_ref)
-    for name, sl in (("W1", slice(0, 256)), ("W2", slice(288, 1312)), ("w3", slice(1344, 1376))):
-        assert rel_l2(g[sl], g_ref[sl]) <= 1e-4, name
-    assert loss == pytest.approx(loss_ref, rel=1e-4)
+    errs = {name: rel_l2(g[sl], g_ref[sl]) for name, sl in (
+        ("all", slice(0, 1377)), ("W1", slice(0, 256)), ("b1", slice(256, 288)), ("W2", slice(288, 1312)),
+        ("b2", slice(1312, 1344)), ("w3", slice(1344, 1376)), ("b3", slice(1376, 1377)))}
+    print(kernel, "gradient vs oracle", errs, "loss", loss, loss_ref)
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, bad
+    assert loss == pytest.approx(loss_ref, rel=tol)
 
 
 def test_training_fits_a_known_closure(pflbm):
