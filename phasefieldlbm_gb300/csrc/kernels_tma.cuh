@@ -75,18 +75,23 @@ __device__ __forceinline__ void normal_pair(const Elem &e, bool va, bool vb, V2 
 __host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~size_t(127); }
 
 // Shared-memory plan of the TMA collide kernel with NS population stages
-// (planes in flight = NS - 1 ahead of the one being collided). Direction q
+// (planes in flight = NS - 1 ahead of the one being collided) and NR planes
+// in the normal ring: 4 lets a warp compute the normals of plane z+1 while
+// others still collide plane z-1 (one block barrier per plane); 3 saves a
+// plane of the ring for one more stage and costs a second barrier per plane
+// (collide_tile_tma). Direction q
 // of plane z comes as one box of TY rows: TX wide at x0 when c_x = 0 (no x
 // halo is read), TX + XU wide otherwise, where XU is the 16-byte alignment
 // unit of the x coordinate, starting at x0 - XU for c_x = +1 (halo column
 // x0 - 1) and at x0 for c_x = -1 (halo column x0 + TX).
-template <int QQ, class S, int NS, class RT = typename Store<S>::T, class G = DefaultTile>
+template <int QQ, class S, int NS, class RT = typename Store<S>::T, class G = DefaultTile, int NR = 4>
 struct TmaPlan {
     using T = typename Store<S>::T;
     using RingT = RT;  // element type of the normal and |grad phi| rings
     using Tile = G;
     static constexpr int TX = G::TX, TY = G::TY, NX_ = G::NX, NY_ = G::NY;
     static constexpr int kStages = NS;
+    static constexpr int kNormSlots = NR;
     static constexpr int XU = 16 / int(sizeof(S));  // elements per 16 bytes
     static constexpr int BWN = TX;                  // box width, c_x = 0
     static constexpr int BWW = TX + XU;             // box width, c_x != 0
@@ -115,9 +120,9 @@ struct TmaPlan {
     static constexpr size_t phi_slot_bytes = align128(phi_plane_bytes);
     static constexpr size_t off_f = 0;
     static constexpr size_t off_phi = align128(NS * stage_bytes);
-    // n^ (3 components) of 4 planes on the tile + halo 1
+    // n^ (3 components) of NR planes on the tile + halo 1
     static constexpr size_t off_n = align128(off_phi + kPhiSlots * phi_slot_bytes);
-    static constexpr size_t n_bytes = size_t(3) * 4 * NY_ * NX_ * sizeof(RT);
+    static constexpr size_t n_bytes = size_t(3) * NR * NY_ * NX_ * sizeof(RT);
     // |grad phi| of 3 planes, tile rows only (rows of the halo width)
     static constexpr size_t off_ind = align128(off_n + n_bytes);
     static constexpr size_t ind_bytes = size_t(3) * TY * NX_ * sizeof(RT);
@@ -131,6 +136,7 @@ struct TmaPlan {
                   "TMA inner box extent");
     static_assert(BWW <= 256 && PBW <= 256 && TY <= 256 && PBH <= 256, "TMA box dimension limit");
     static_assert(NS >= 2 && NS * 8 + 4 <= 64, "mbarrier area");
+    static_assert(NR == 3 || NR == 4, "normal ring planes");
 };
 
 // Deepest pipeline (4, 3 or 2 stages) that keeps two CTAs per SM (FP32 and
@@ -162,13 +168,17 @@ struct TmaStages {
                                       : CollideOccupancy<QQ, S>::value == 3 ? 74u * 1024u
                                                                             : size_t(PFLBM_TMA_SMEM_BUDGET);
     using RT = typename Store<S>::T;
-    static constexpr int value = TmaPlan<QQ, S, 4, RT, G>::total <= kBudget   ? 4
-                                 : TmaPlan<QQ, S, 3, RT, G>::total <= kBudget ? 3
-                                                                              : 2;
+    // a third stage with the 3-plane normal ring where the 4-plane ring
+    // leaves room for two stages only (D3Q27 with FP32 storage)
+    static constexpr bool kDeep4 = TmaPlan<QQ, S, 4, RT, G>::total <= kBudget;
+    static constexpr bool kMid4 = TmaPlan<QQ, S, 3, RT, G>::total <= kBudget;
+    static constexpr bool kMid3 = TmaPlan<QQ, S, 3, RT, G, 3>::total <= kBudget;
+    static constexpr int value = kDeep4 ? 4 : (kMid4 || kMid3) ? 3 : 2;
+    static constexpr int rings = (kDeep4 || kMid4 || !kMid3) ? 4 : 3;
 };
 
 template <int QQ, class S, class G = DefaultTile>
-using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S, G>::value, typename Store<S>::T, G>;
+using TmaLayout = TmaPlan<QQ, S, TmaStages<QQ, S, G>::value, typename Store<S>::T, G, TmaStages<QQ, S, G>::rings>;
 
 // The closure modes place the network after the pipeline's shared memory:
 // their pipeline is the deepest whose plan plus the network still fits the
@@ -235,7 +245,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
     T *s_phi = reinterpret_cast<T *>(smem + L::off_phi);
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);
     T *s_ind = reinterpret_cast<T *>(smem + L::off_ind);
-    constexpr int NS = L::kStages, R = L::kPhiSlots;
+    constexpr int NS = L::kStages, R = L::kPhiSlots, NR = L::kNormSlots;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
     volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L::off_bar + 8 * NS);
 
@@ -250,7 +260,8 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         return *reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(s_phi) + slot * L::phi_slot_bytes +
                                       (size_t(ly) * L::PBW + lx) * sizeof(T));
     };
-    auto n_at = [&](int c, int slot, int ly, int lx) -> T & { return s_n[((c * 4 + slot) * NY_ + ly) * NX_ + lx]; };
+    auto n_at = [&](int c, int slot, int ly, int lx) -> T & { return s_n[((c * NR + slot) * NY_ + ly) * NX_ + lx]; };
+    auto nslot = [](int zp) { return (zp + NR) % NR; };  // normal ring slot of plane zp (zp >= -1)
     // |grad phi| of plane zp at tile row r, halo column lx (slot zp % 3)
     auto ind_at = [&](int zp, int r, int lx) -> T & { return s_ind[((zp % 3) * TY + r) * NX_ + lx]; };
     auto issue = [&](int stage, int zf) {
@@ -288,7 +299,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
     fence_proxy_async();
     auto compute_n = [&](int zp) {
         const int sn = pslot(zp), sm = pslot(zp - 1), sp = pslot(zp + 1);
-        const int nn = (zp + 4) & 3;  // normal ring slot
+        const int nn = nslot(zp);
         if constexpr (sizeof(T) == 4) {
             // two x-adjacent entries per thread: 170 entry pairs, at most one
             // per thread, so no warp computes a second round
@@ -341,8 +352,14 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         const int st = int(sq % NS);
         const uint32_t par = (sq / NS) & 1;
         if (!plane_wait<L>(smem, &bar[st], par)) *s_abort = 1;
-        compute_n(z + 1);
-        __syncthreads();
+        if constexpr (NR == 3) {
+            // the ring slot of plane z+1 is that of plane z-2, which the
+            // collision of plane z-1 reads: every warp has left it here
+            __syncthreads();
+        } else {
+            compute_n(z + 1);
+            __syncthreads();
+        }
         if (*s_abort) {
             if (tid == 0) {
                 atomicOr(b.err, 1u);
@@ -354,11 +371,15 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
         }
         // plane z+NS-1 goes into the stage of plane z-1, consumed last iteration
         if (tid == 0 && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
+        if constexpr (NR == 3) {
+            compute_n(z + 1);
+            __syncthreads();
+        }
         // the tensor-core closure network needs every lane of the warp
         constexpr bool kWarpWide = mode_closure(MODE) && std::is_same<T, float>::value;
         if (!col && !kWarpWide) continue;
 
-        const int s_m = (z + 3) & 3, s_0 = z & 3, s_p = (z + 1) & 3;
+        const int s_m = nslot(z - 1), s_0 = nslot(z), s_p = nslot(z + 1);
         auto nv = [&](int c, int dx, int dy, int dz) -> T {
             return n_at(c, dz < 0 ? s_m : (dz > 0 ? s_p : s_0), ty + 1 + dy, tx + 1 + dx);
         };
