@@ -208,16 +208,16 @@ __device__ __forceinline__ void phase_vec4(const Params<float> &p, const StepBuf
         s += w1 * (a_zp[k] - b_zp[k]);
         out[k] = s;
     }
-    // ghost columns keep their (zero) phi; write only interior nodes
+    // the ghost columns keep their phi (both ping-pong buffers hold the same
+    // initial ghost values): the source's value is stored again with the
+    // row's end segments, so that every row is written by whole 16-byte
+    // stores and no 32-byte sector of it is left partly written, which the
+    // memory system completes with a read of the old sector (0.045 -> 0.043
+    // ms on the 128x128x512 jet)
     if (!PFLBM_GUARD(r0 + x4 + 3 < N, b.err)) return;
-    if (x4 >= 1 && x4 + 3 <= nx - 2) {
-        *reinterpret_cast<float4 *>(b.phi_dst + r0 + x4) = make_float4(out[0], out[1], out[2], out[3]);
-    } else {
-        for (int k = 0; k < 4; ++k) {
-            const int x = x4 + k;
-            if (x >= 1 && x <= nx - 2) b.phi_dst[r0 + x] = out[k];
-        }
-    }
+    if (x4 == 0) out[0] = pc.x;
+    if (x4 + 3 == nx - 1) out[3] = pc.w;
+    *reinterpret_cast<float4 *>(b.phi_dst + r0 + x4) = make_float4(out[0], out[1], out[2], out[3]);
 }
 
 // FP32 phase step with 128-bit accesses: one thread owns 4 consecutive x
