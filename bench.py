@@ -517,6 +517,7 @@ def run_closure_study(args) -> dict:
                 cl.add_snapshot(fine, stride=stride)
             ref = {f: restrict_filtered(fine.get_field(f)) for f in ("avg_uz", "avg_phi")}
         out["samples"] = cl.num_samples
+        out["interface"] = {k: round(v, 4) for k, v in cl.interface_scale().items()}
         out["t_fine_s"] = round(time.perf_counter() - t0, 1)
         cl.init_params(seed=args.seed)
         loss0 = cl.loss()
@@ -527,8 +528,9 @@ def run_closure_study(args) -> dict:
                         "seconds": round(time.perf_counter() - t1, 2)}
         blob = cl.blob
 
-    def coarse_run(strength, mixing=0.0):
-        c = coarse_cfg
+    def coarse_run(strength, mixing=0.0, gamma_scale=1.0):
+        c = coarse_cfg.copy()
+        c.gamma = float(np.float32(c.gamma * gamma_scale))
         with pf.Simulation(c) as s:
             if strength > 0:
                 s.set_closure(blob, strength)
@@ -549,12 +551,20 @@ def run_closure_study(args) -> dict:
                                          np.linalg.norm(ref[f][2:-2, cy, cx]))
         return e
 
+    # the closure: the learned eddy viscosity and the interface sharpening
+    # scaled to the filtered fine interface width; each part alone as well
+    gs = out["interface"]["gamma_scale"]
     runs = {}
-    cases = [("plain", 0.0, 0.0), ("closure", 1.0, 0.0)] + [(f"closure_x{v:g}", v, 0.0) for v in args.extra_strengths]
-    cases += [(f"closure_mix{m:g}", 1.0, m) for m in args.mixing]
-    for name, strength, mixing in cases:
-        res, mlups = coarse_run(strength, mixing)
-        runs[name] = {"strength": strength, "mixing": mixing, "mlups": round(mlups, 1), **errors(res)}
+    cases = [("plain", 0.0, 0.0, 1.0), ("closure", 1.0, 0.0, gs), ("closure_nu_only", 1.0, 0.0, 1.0),
+             ("plain_sharpened", 0.0, 0.0, gs)]
+    cases += [(f"closure_x{v:g}", v, 0.0, gs) for v in args.extra_strengths]
+    cases += [(f"closure_nu_only_mix{m:g}", 1.0, m, 1.0) for m in args.mixing]
+    for g in args.gamma_scales:
+        cases += [(f"plain_gamma{g:g}", 0.0, 0.0, g), (f"closure_gamma{g:g}", 1.0, 0.0, g)]
+    for name, strength, mixing, gs in cases:
+        res, mlups = coarse_run(strength, mixing, gs)
+        runs[name] = {"strength": strength, "mixing": mixing, "gamma_scale": gs, "mlups": round(mlups, 1),
+                      **errors(res)}
     out["runs"] = runs
     out["seconds"] = round(time.perf_counter() - t0, 1)
     return out
@@ -628,8 +638,10 @@ def main():
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--extra-strengths", type=float, nargs="*", default=[0.5, 2.0])
-    ap.add_argument("--mixing", type=float, nargs="*", default=[1.0, 2.0, 4.0],
+    ap.add_argument("--mixing", type=float, nargs="*", default=[1.0],
                     help="closure study: inverse turbulent Schmidt numbers of the phase mixing")
+    ap.add_argument("--gamma-scales", type=float, nargs="*", default=[],
+                    help="closure study: coarse-grid multipliers of the interface sharpening gamma")
     ap.add_argument("--checkpoints", default="500,1000,2000,5000,10000")
     args = ap.parse_args()
     if args.study:

@@ -329,6 +329,17 @@ int pflbm_closure_create(int32_t device, uint64_t max_samples, pflbm_closure **o
  * with x and y multiples of stride, all interior z). */
 int pflbm_closure_add_snapshot(pflbm_closure *c, pflbm_sim *fine, int32_t stride, uint64_t *added);
 int pflbm_closure_num_samples(const pflbm_closure *c, uint64_t *n);
+/* Interface width of the snapshots added so far, W = 4 sum phi(1-phi) /
+ * sum |grad phi| over the sample nodes: on the fine field at the samples'
+ * fine nodes (fine lattice units) and on the filtered coarse field (coarse
+ * units). gamma_scale = width_fine / width_filtered is the factor on the
+ * coarse run's interface sharpening gamma that gives its equilibrium
+ * interface the filtered fine width (W ~ 1 / gamma at the fixed mobility of
+ * tau_g = 1); the phase-field part of the closure. widths may be NULL.
+ * PFLBM_ERR_STATE when the snapshots hold no interface. Samples replaced by
+ * set_samples keep the widths of the snapshots added before. */
+int pflbm_closure_interface_scale(const pflbm_closure *c, double *gamma_scale, double *width_fine,
+                                  double *width_filtered);
 /* Samples as host arrays x[n][8], y[n]; set_samples replaces the data set. */
 int pflbm_closure_get_samples(pflbm_closure *c, uint64_t first, uint64_t count, float *host_x, float *host_y);
 int pflbm_closure_set_samples(pflbm_closure *c, const float *host_x, const float *host_y, uint64_t count);

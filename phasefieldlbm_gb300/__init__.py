@@ -54,6 +54,7 @@ EXPORTED_SYMBOLS = [
     "pflbm_ensemble_info", "pflbm_ensemble_destroy", "pflbm_ensemble_set_tile", "pflbm_ensemble_get_tuning",
     "pflbm_reduce_fields_noalloc", "pflbm_write_output_async", "pflbm_set_watchdog",
     "pflbm_closure_create", "pflbm_closure_add_snapshot", "pflbm_closure_num_samples", "pflbm_closure_get_samples",
+    "pflbm_closure_interface_scale",
     "pflbm_closure_set_samples", "pflbm_closure_init_params", "pflbm_closure_get_blob", "pflbm_closure_set_blob",
     "pflbm_closure_gradient", "pflbm_closure_train", "pflbm_closure_loss", "pflbm_closure_destroy",
     "pflbm_set_closure", "pflbm_set_closure_mixing",
@@ -191,6 +192,7 @@ def load_library(path: str | os.PathLike | None = None, build_if_missing: bool =
         "pflbm_closure_create": ([i32, u64, ctypes.POINTER(vp)], ctypes.c_int),
         "pflbm_closure_add_snapshot": ([vp, vp, i32, ctypes.POINTER(u64)], ctypes.c_int),
         "pflbm_closure_num_samples": ([vp, ctypes.POINTER(u64)], ctypes.c_int),
+        "pflbm_closure_interface_scale": ([vp] + [ctypes.POINTER(ctypes.c_double)] * 3, ctypes.c_int),
         "pflbm_closure_get_samples": ([vp, u64, u64, vp, vp], ctypes.c_int),
         "pflbm_closure_set_samples": ([vp, vp, vp, u64], ctypes.c_int),
         "pflbm_closure_init_params": ([vp, u32], ctypes.c_int),
@@ -583,6 +585,16 @@ class Closure:
         n = ctypes.c_uint64()
         _check(self.lib, self.lib.pflbm_closure_num_samples(self._h, ctypes.byref(n)))
         return int(n.value)
+
+    def interface_scale(self) -> dict:
+        """Interface widths of the snapshots (fine field in fine units,
+        filtered field in coarse units) and gamma_scale = their ratio, the
+        factor on a coarse run's interface sharpening gamma that gives it
+        the filtered fine interface width."""
+        g, wf, wc = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(self.lib, self.lib.pflbm_closure_interface_scale(self._h, ctypes.byref(g), ctypes.byref(wf),
+                                                                 ctypes.byref(wc)))
+        return {"gamma_scale": g.value, "width_fine": wf.value, "width_filtered": wc.value}
 
     def samples(self, first: int = 0, count: int | None = None):
         count = self.num_samples - first if count is None else count

@@ -21,6 +21,16 @@
 //            coarse solver carries, Chapman-Enskog, tau0 its molecular
 //            relaxation time), phi, |grad phi| (D3Q19 lattice gradient, as
 //            the solver's normals stencil).
+//
+// Interface width. The same sample nodes give the thickness of the phase
+// interface: for a tanh profile, sum phi (1 - phi) / sum |grad phi| is a
+// quarter of the width W. Measured on the filtered coarse field (coarse
+// units) and on the fine field at the sample's fine node 2X (fine units, the
+// solver's own |grad phi|), their ratio is the factor by which the coarse
+// run's interface sharpening gamma must grow for its equilibrium interface
+// (W proportional to 1 / gamma at the fixed phase mobility) to have the
+// filtered fine width; the coarse grid otherwise resolves an interface twice
+// as thick in physical units.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -111,11 +121,19 @@ __global__ void k_filter_restrict(const float *__restrict__ macro, uint64_t Nf, 
 
 // Samples at coarse nodes 2 <= i,j,k <= n-3 with i % stride == 0 and
 // j % stride == 0, written in (k, j, i) order from `base`.
-__global__ void k_make_samples(const float *__restrict__ coarse, int nxc, int nyc, int nzc, int stride, float tau_w,
-                               float tau_o, int i0, int ni, int j0, int nj, float *__restrict__ X,
-                               float *__restrict__ Y, uint64_t base) {
+// Each block also writes its sums of phi(1-phi) and |grad phi| on the
+// filtered coarse field and on the fine field at 2X (width[blockIdx.x * 4 +
+// 0..3], FP64, summed in block order on the host).
+constexpr int kMakeThreads = 256, kMakeBlocks = 1216;
+__global__ void __launch_bounds__(kMakeThreads) k_make_samples(const float *__restrict__ coarse, int nxc, int nyc,
+                                                               int nzc, int stride, float tau_w, float tau_o, int i0,
+                                                               int ni, int j0, int nj, float *__restrict__ X,
+                                                               float *__restrict__ Y, uint64_t base,
+                                                               const float *__restrict__ macro, uint64_t Nf, int nxf,
+                                                               int nyf, double *__restrict__ width) {
     const uint64_t Nc = uint64_t(nxc) * nyc * nzc;
     const uint64_t total = uint64_t(ni) * nj * (nzc - 4);
+    double wsum[4] = {0.0, 0.0, 0.0, 0.0};
     for (uint64_t s = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; s < total; s += uint64_t(gridDim.x) * blockDim.x) {
         const int ii = int(s % ni), jj = int((s / ni) % nj), kk = int(s / (uint64_t(ni) * nj));
         const int i = i0 + ii * stride, j = j0 + jj * stride, k = 2 + kk;
@@ -160,7 +178,22 @@ __global__ void k_make_samples(const float *__restrict__ coarse, int nxc, int ny
         x[3] = c * sxy; x[4] = c * sxz; x[5] = c * syz;
         x[6] = phi; x[7] = ind;
         Y[base + s] = nu;
+        const uint64_t f = uint64_t(2 * i) + uint64_t(nxf) * (uint64_t(2 * j) + uint64_t(nyf) * uint64_t(2 * k));
+        const double phf = macro[pflbm::M_PHI * Nf + f], indf = macro[pflbm::M_IND * Nf + f];
+        wsum[0] += double(phi) * (1.0 - double(phi));
+        wsum[1] += double(ind);
+        wsum[2] += phf * (1.0 - phf);
+        wsum[3] += indf;
     }
+    __shared__ double red[4][kMakeThreads];
+    for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = wsum[q];
+    __syncthreads();
+    for (int h = kMakeThreads / 2; h > 0; h >>= 1) {
+        if (int(threadIdx.x) < h)
+            for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) width[blockIdx.x * 4 + threadIdx.x] = red[threadIdx.x][0];
 }
 
 // FP64 sums of x_k, x_k^2 (k < 8), y, y^2 per block.
@@ -617,13 +650,15 @@ struct pflbm_closure {
     int loss_log_cap = 0;
     float *coarse = nullptr;
     uint64_t coarse_cap = 0;
+    double *width_part = nullptr;           // per-block interface sums of a snapshot
+    double width_sum[4] = {0, 0, 0, 0};     // phi(1-phi), |grad phi|: filtered coarse, fine
     uint64_t adam_t = 0;
     bool have_params = false;
     std::vector<float> host_blob = std::vector<float>(kMlpBlob, 0.0f);
 
     ~pflbm_closure() {
         cudaSetDevice(device);
-        void *ptrs[] = {X, Y, blob, m, v, gpart, grad, partial, loss_log, coarse};
+        void *ptrs[] = {X, Y, blob, m, v, gpart, grad, partial, loss_log, coarse, width_part};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
@@ -702,7 +737,8 @@ int pflbm_closure_create(int32_t device, uint64_t max_samples, pflbm_closure **o
         cudaMalloc(&c->m, sizeof(float) * kMlpParams) != cudaSuccess ||
         cudaMalloc(&c->v, sizeof(float) * kMlpParams) != cudaSuccess ||
         cudaMalloc(&c->grad, sizeof(double) * (kMlpParams + 1)) != cudaSuccess ||
-        cudaMalloc(&c->partial, sizeof(double) * kLossBlocks * 18) != cudaSuccess) {
+        cudaMalloc(&c->partial, sizeof(double) * kLossBlocks * 18) != cudaSuccess ||
+        cudaMalloc(&c->width_part, sizeof(double) * kMakeBlocks * 4) != cudaSuccess) {
         cudaGetLastError();
         return fail(PFLBM_ERR_OUT_OF_MEMORY, "closure buffers");
     }
@@ -758,12 +794,31 @@ int pflbm_closure_add_snapshot(pflbm_closure *c, pflbm_sim *fine, int32_t stride
     // the fine run's analysis ran on its own stream, which sim_view synchronised
     k_filter_restrict<<<1216, 256, 0, c->stream>>>(static_cast<const float *>(v.macro), v.N, int(v.nx), int(v.ny),
                                                    int(v.nz), nxc, nyc, nzc, c->coarse);
-    k_make_samples<<<1216, 256, 0, c->stream>>>(c->coarse, nxc, nyc, nzc, stride, float(v.tau_water),
-                                                float(v.tau_oil), i0, ni, j0, nj, c->X, c->Y, c->n);
-    cudaError_t e = cudaStreamSynchronize(c->stream);
+    k_make_samples<<<kMakeBlocks, kMakeThreads, 0, c->stream>>>(
+        c->coarse, nxc, nyc, nzc, stride, float(v.tau_water), float(v.tau_oil), i0, ni, j0, nj, c->X, c->Y, c->n,
+        static_cast<const float *>(v.macro), v.N, int(v.nx), int(v.ny), c->width_part);
+    std::vector<double> wp(size_t(kMakeBlocks) * 4);
+    cudaError_t e = cudaMemcpyAsync(wp.data(), c->width_part, sizeof(double) * wp.size(), cudaMemcpyDeviceToHost,
+                                    c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "closure snapshot");
+    for (int b = 0; b < kMakeBlocks; ++b)
+        for (int q = 0; q < 4; ++q) c->width_sum[q] += wp[size_t(b) * 4 + q];
     c->n += count;
     if (added) *added = count;
+    return PFLBM_OK;
+}
+
+int pflbm_closure_interface_scale(const pflbm_closure *c, double *gamma_scale, double *width_fine,
+                                   double *width_filtered) {
+    if (!c || !gamma_scale) return fail(PFLBM_ERR_INVALID_ARG, "null argument");
+    const double *w = c->width_sum;
+    if (!(w[0] > 0.0 && w[1] > 0.0 && w[2] > 0.0 && w[3] > 0.0))
+        return fail(PFLBM_ERR_STATE, "no interface in the snapshots added so far");
+    const double wc = 4.0 * w[0] / w[1], wf = 4.0 * w[2] / w[3];
+    *gamma_scale = wf / wc;
+    if (width_fine) *width_fine = wf;
+    if (width_filtered) *width_filtered = wc;
     return PFLBM_OK;
 }
 

@@ -266,12 +266,13 @@ def _jet_closure_pair(pflbm, nx, nz, diam):
 
 
 def test_trained_closure_beats_constant_tau(pflbm):
-    """The learned part end to end at a small scale: snapshots of a 2x-finer
-    run of the same seeded jet (Re = 10000), GPU training, then coarse runs
-    with and without the closure judged by the relative L2 error of their
-    time-averaged u_z and phi against the filtered fine average: the closure
-    must lower both errors (measured 0.447 -> 0.387 on <u_z>, 0.2276 ->
-    0.2258 on <phi>)."""
+    """The closure end to end at a small scale: snapshots of a 2x-finer run
+    of the same seeded jet (Re = 10000), GPU training of the eddy-viscosity
+    network and the interface width of the snapshots, then coarse runs judged
+    by the relative L2 error of their time-averaged u_z and phi against the
+    filtered fine average. The closure (network + sharpening scaled to the
+    filtered fine interface width) must lower both errors, and each part must
+    help on its own quantity."""
     fine_cfg, coarse_cfg = _jet_closure_pair(pflbm, 96, 384, 12)
     snaps, every = 10, 200
     with pflbm.Closure(2_000_000) as cl:
@@ -285,18 +286,53 @@ def test_trained_closure_beats_constant_tau(pflbm):
         cl.train(1000, batch=16384, lr=2e-3, seed=2026)
         l1 = cl.loss()
         blob = cl.blob
+        iface = cl.interface_scale()
     assert l1 < l0
+    # the coarse grid resolves the interface about twice as thick (physical
+    # units); the box filter broadens the filtered one a little
+    assert 1.2 < iface["gamma_scale"] < 2.2, iface
     err = {}
-    for name, strength in (("plain", 0.0), ("closure", 1.0)):
-        with pflbm.Simulation(coarse_cfg) as s:
+    for name, strength, gs in (("plain", 0.0, 1.0), ("nu_only", 1.0, 1.0), ("closure", 1.0, iface["gamma_scale"])):
+        c = coarse_cfg.copy()
+        c.gamma = float(np.float32(c.gamma * gs))
+        with pflbm.Simulation(c) as s:
             if strength:
                 s.set_closure(blob, strength)
             s.step(snaps * every // 2)
             sl = (slice(2, -2),) * 3
             err[name] = {f: rel_l2(s.get_field(f).astype(np.float64)[sl], ref[f][sl]) for f in ("avg_uz", "avg_phi")}
-    print("training loss", l0, "->", l1, "errors", err)
+    print("training loss", l0, "->", l1, "interface", iface, "errors", err)
+    assert err["nu_only"]["avg_uz"] < err["plain"]["avg_uz"]
     assert err["closure"]["avg_uz"] < err["plain"]["avg_uz"]
-    assert err["closure"]["avg_phi"] < err["plain"]["avg_phi"]
+    assert err["closure"]["avg_phi"] < err["nu_only"]["avg_phi"] < err["plain"]["avg_phi"]
+
+
+def test_interface_width_of_snapshots(pflbm):
+    """pflbm_closure_interface_scale: the widths 4 sum phi(1-phi) / sum
+    |grad phi| over the sample nodes, recomputed on the host from the
+    samples' features (filtered field) and from the fine run's own phi and
+    |grad phi| at the samples' fine nodes 2X."""
+    fine_cfg, _ = _jet_closure_pair(pflbm, 64, 256, 10)
+    with pflbm.Closure(400_000) as cl:
+        with pflbm.Simulation(fine_cfg) as fine:
+            fine.step(300)
+            cl.add_snapshot(fine, stride=2)
+            phi = fine.get_field("phi").astype(np.float64)
+            ind = fine.get_field("ind").astype(np.float64)
+        x, _ = cl.samples()
+        got = cl.interface_scale()
+    xf = x.astype(np.float64)
+    w_filtered = 4.0 * np.sum(xf[:, 6] * (1.0 - xf[:, 6])) / np.sum(xf[:, 7])
+    nzc, nyc, nxc = (n // 2 for n in phi.shape)
+    i = np.arange(2, nxc - 2, 2)  # the sample lattice of stride 2
+    k = np.arange(2, nzc - 2)
+    pf_ = phi[2 * k][:, 2 * i][:, :, 2 * i]
+    if_ = ind[2 * k][:, 2 * i][:, :, 2 * i]
+    w_fine = 4.0 * np.sum(pf_ * (1.0 - pf_)) / np.sum(if_)
+    assert x.shape[0] == len(k) * len(i) * len(i)
+    assert got["width_filtered"] == pytest.approx(w_filtered, rel=1e-5)
+    assert got["width_fine"] == pytest.approx(w_fine, rel=1e-5)
+    assert got["gamma_scale"] == pytest.approx(w_fine / w_filtered, rel=1e-5)
 
 
 @pytest.mark.parametrize("storage,avg", [(0, 0), (0, 1), (3, 0)])
