@@ -335,6 +335,16 @@ def test_interface_width_of_snapshots(pflbm):
     assert got["gamma_scale"] == pytest.approx(w_fine / w_filtered, rel=1e-5)
 
 
+def test_interface_scale_needs_snapshots_with_an_interface(pflbm):
+    """Samples supplied by the caller carry no interface widths: the scale is
+    refused with PFLBM_ERR_STATE until a snapshot with an interface is added."""
+    with pflbm.Closure(4096) as c:
+        c.set_samples(_features(4096, 3), np.full(4096, 1e-3))
+        with pytest.raises(pflbm.PflbmError) as e:
+            c.interface_scale()
+        assert e.value.code == 4, e.value
+
+
 @pytest.mark.parametrize("storage,avg", [(0, 0), (0, 1), (3, 0)])
 def test_closure_on_tma_and_plain_kernels_bit_identical(pflbm, monkeypatch, storage, avg):
     """The closure-coupled step runs on the TMA-fed collide when rows are
