@@ -246,6 +246,12 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);
     T *s_ind = reinterpret_cast<T *>(smem + L::off_ind);
     constexpr int NS = L::kStages, R = L::kPhiSlots, NR = L::kNormSlots;
+    // The thread that issues the TMA copies: in the last warp when no lane
+    // of that warp computes normal-ring entries, so that with the 3-plane
+    // ring the copies are issued while the other warps compute the normals
+    // between the plane's two barriers, not by a warp on that critical path.
+    constexpr int kNormWork = sizeof(T) == 4 ? NXP * NY_ : NX_ * NY_;
+    constexpr int kIssuer = kNormWork <= NT - 32 ? NT - 32 : 0;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::off_bar);
     volatile int *s_abort = reinterpret_cast<volatile int *>(smem + L::off_bar + 8 * NS);
 
@@ -343,7 +349,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
     __syncthreads();
     // stages 0 .. NS-2 (planes zb .., phi zb+2 ..); the phi ring slot of
     // plane zb+NS aliases that of zb-2, which compute_n(zb-1) no longer needs
-    if (tid == 0)
+    if (tid == kIssuer)
         for (int k = 0; k < NS - 1 && zb + k < ze; ++k) issue((seq + k) % NS, zb + k);
     compute_n(zb);
 
@@ -370,7 +376,7 @@ __device__ __forceinline__ bool collide_tile_tma(const Params<typename Store<S>:
             return false;
         }
         // plane z+NS-1 goes into the stage of plane z-1, consumed last iteration
-        if (tid == 0 && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
+        if (tid == kIssuer && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
         if constexpr (NR == 3) {
             compute_n(z + 1);
             __syncthreads();
