@@ -176,7 +176,7 @@ def cpu_oracle_mlups(cfg, steps: int, warm: int = 1) -> tuple[float, float, int]
 # interior planes swept (510 / 126;
 # profiles/k_collide_tma_jet_d3q19_fp32_128x128x128.md).
 NCU_COLLIDE_TRAFFIC = {
-    "jet_d3q27": ((1026.117888e6 + 938.388224e6) + (1025.818624e6 + 935.277824e6)) / 2,
+    "jet_d3q27": ((1026.005248e6 + 938.875136e6) + (1026.161664e6 + 935.919616e6)) / 2,
     "jet_d3q19": (179.217664e6 + 127.435776e6) * 510 / 126,
 }
 NCU_TRAFFIC_SOURCE = {
