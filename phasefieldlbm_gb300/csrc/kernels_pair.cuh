@@ -482,6 +482,12 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
     T *s_n = reinterpret_cast<T *>(smem + L::off_n);
     T *s_ind = reinterpret_cast<T *>(smem + L::off_ind);
     constexpr int NS = L::kStages, R = L::kPhiSlots;
+    // The thread that issues the TMA copies: the last warp's first lane,
+    // when that warp computes fewer normal-ring pairs per plane than the
+    // first (170 pairs on 128 threads: threads 0 - 41 compute two), so that
+    // the copies issued after the plane's barrier are absorbed by its slack
+    // before the next barrier.
+    constexpr int kIssuer = ((NXP * NY_) % NT2) <= NT2 - 32 ? NT2 - 32 : 0;
     // c_x = 0 boxes: element 2 i2 of an even-width row, an aligned pair
     static_assert(L::PXO % 2 == 0 && L::BWN % 2 == 0 && L::BWW % 2 == 0 && L::XU % 2 == 0 && L::PBW % 2 == 0,
                   "pair alignment");
@@ -559,7 +565,7 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
     __syncthreads();
     compute_n(zb - 1);
     __syncthreads();
-    if (tid == 0)
+    if (tid == kIssuer)
         for (int k = 0; k < NS - 1 && zb + k < ze; ++k) issue((seq + k) % NS, zb + k);
     compute_n(zb);
 
@@ -578,7 +584,7 @@ __device__ __forceinline__ bool collide_tile_pair(const Params<float> &p, const 
             }
             return false;
         }
-        if (tid == 0 && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
+        if (tid == kIssuer && z + NS - 1 < ze) issue(int((sq + NS - 1) % NS), z + NS - 1);
         if (!(act_a || act_b)) continue;
 
         const int s_m = (z + 3) & 3, s_0 = z & 3, s_p = (z + 1) & 3;
