@@ -43,7 +43,7 @@ def _with_u(d):
     return d
 
 
-def _fp32_verdict(lib, ora32, ora64):
+def _fp32_errors_against_floor(lib, ora32, ora64):
     lib, ora32, ora64 = _with_u(lib), _with_u(ora32), _with_u(ora64)
     e = {f: rel_l2(lib[f], ora32[f]) for f in BASIC + ("u",)}
     floor = {f: rel_l2(ora32[f], ora64[f]) for f in BASIC + ("u",)}
@@ -79,7 +79,7 @@ def test_bench_jet_d3q27_preset_against_oracle(pflbm, oracle):
     assert max(e64.values()) <= 1e-10, e64
     ora32 = _oracle_run(oracle, cfg, steps, False, BASIC)
     lib32 = _lib_run(pflbm, cfg, pflbm.STORAGE_FP32, steps, BASIC)
-    e, floor, bad = _fp32_verdict(lib32, ora32, {f: ora64[f] for f in BASIC})
+    e, floor, bad = _fp32_errors_against_floor(lib32, ora32, {f: ora64[f] for f in BASIC})
     print("jet_d3q27 preset FP32 vs FP32 oracle", e, "floor", floor)
     assert not bad, (bad, e, floor)
 
@@ -90,7 +90,7 @@ def test_droplet64_full_run_against_oracle(pflbm, oracle):
     ora32 = _oracle_run(oracle, cfg, steps, False, BASIC)
     ora64 = _oracle_run(oracle, cfg, steps, True, BASIC)
     lib32 = _lib_run(pflbm, cfg, pflbm.STORAGE_FP32, steps, BASIC)
-    e, floor, bad = _fp32_verdict(lib32, ora32, ora64)
+    e, floor, bad = _fp32_errors_against_floor(lib32, ora32, ora64)
     print("droplet64 1000 steps FP32 vs FP32 oracle", e, "floor", floor)
     assert not bad, (bad, e, floor)
     # phase mass of the oracle run conserved as the library's is
@@ -111,6 +111,6 @@ def test_ensemble_boxes_at_real_size_against_oracle(pflbm, oracle):
         c = batch[k]
         ora32 = _oracle_run(oracle, c, steps, False, BASIC)
         ora64 = _oracle_run(oracle, c, steps, True, BASIC)
-        e, floor, bad = _fp32_verdict(got[k], ora32, ora64)
+        e, floor, bad = _fp32_errors_against_floor(got[k], ora32, ora64)
         print(f"ensemble box {pick[k]} (edge {int(c.nx)}) FP32 vs FP32 oracle", e, "floor", floor)
         assert not bad, (int(c.nx), bad, e, floor)
