@@ -13,10 +13,13 @@
 //   * phi: one 3D tensor map, box 40 x 12 (tile + halo 2) at (x0-4, y0-2),
 //     two planes ahead of the plane the stage carries, into a ring of NS+2
 //     slots.
-// Both arrive on one mbarrier per stage (expect_tx), issued by thread 0 right
-// after the block barrier that ends the use of the stage's previous plane.
-// Out-of-range boxes are zero-filled by the TMA unit; those elements only
-// feed ghost nodes, which are never updated. One __syncthreads per plane.
+// Both arrive on one mbarrier per stage (expect_tx), issued by one thread
+// (the last warp's first lane when that warp computes no normal-ring
+// entries, else thread 0) right after the block barrier that ends the use of
+// the stage's previous plane. Out-of-range boxes are zero-filled by the TMA
+// unit; those elements only feed ghost nodes, which are never updated. One
+// __syncthreads per plane with the 4-plane normal ring, two with the
+// 3-plane ring (collide_tile_tma).
 //
 // Every mbarrier wait is bounded; on a timeout the CTA records an error in
 // the device error word, drains its own copies (bounded) and returns as a
